@@ -1,0 +1,400 @@
+"""Benchmark of libbhgpu's per-step Barnes-Hut pipeline (one JSON line on stdout).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+Default workload ("plummer-4m"): one Plummer sphere, N = 2^22 bodies (FP32 state), theta 0.5,
+softening 0.005, leaf capacity 16, dt 5e-4, root edge 2S, quadrupole multipoles. A step is one
+full frame of the reference's sequence: bounds, Morton keys, sort, kick+drift, tree build,
+upsweep, walk + force, kick.
+
+  value  body-steps/s over K timed steps with the state resident in HBM; every step is
+         bracketed by CUDA events on the library's stream and the L2 is flushed between steps
+         (outside the events); the per-step working set (~0.6 GB) is also larger than L2.
+  e2e    the same metric through the C ABI with host buffers: upload (pinned host -> device),
+         one bh_step, download of positions and velocities, CUDA events around all of it.
+  roofline  the tree walk (the dominant kernel) against the measured FP32 FMA peak of this GPU
+         (bh_measure_fp32_peak); the Morton sort against MEASURED_PEAKS.json's HBM copy peak.
+  cpu_baseline  the oracle port of the reference's serial path on this host's cores (1 thread,
+         as the reference), on a bounded sample: the full tree build over all N bodies plus the
+         walk of a seeded subsample, extrapolated to N (stated in "sample").
+
+--impl reference: the reference's CPU implementation of the same step (the oracle port: the
+reference's own sources cannot be compiled on this machine), with all host threads.
+Multi-GPU (torchrun): independent replicas, one per GPU (the single-system step does not
+shard); value = sum of per-rank body-steps / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "plummer-4m": dict(n=1 << 22, theta=0.5, eps=0.005, leaf=16, dt=5e-4, edge=2.0, kind="plummer", seed=0,
+                       desc="Plummer sphere N=2^22, theta=0.5, eps=0.005, leaf 16, dt=5e-4, quadrupole, edge 2S"),
+    "plummer-16k": dict(n=16384, theta=0.5, eps=0.01, leaf=1, dt=1e-3, edge=2.0, kind="plummer", seed=0,
+                        desc="Plummer sphere N=16384, theta=0.5, eps=0.01, leaf 1, dt=1e-3, quadrupole, edge 2S"),
+    "two-spheres-4m": dict(n=1 << 22, theta=0.5, eps=0.001, leaf=8, dt=2e-4, edge=2.0, kind="two", seed=0,
+                           desc="two Plummer spheres of 2^21 (B: a=0.1, M=0.1 at (10,0,0)), theta=0.5, "
+                                "eps=0.001, leaf 8, dt=2e-4"),
+}
+METRIC = "body-steps/s @theta=0.5, acc err<=1e-3: plain vs batched/adjoint, 1 GB300 vs CPU"
+FLOPS_P2P, FLOPS_CELL_QUAD = 20, 57  # per interaction, see the design doc (FMA = 2 flops)
+SORT_PASSES = 8
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.ws == 1:
+            return x
+        import torch
+
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.ws == 1:
+            return x
+        import torch
+
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+
+def make_inputs(bh, w, seed):
+    if w["kind"] == "two":
+        return bh.two_spheres(seed, w["n"])
+    return bh.plummer(seed, w["n"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.f:
+            return None
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    idx = int(parts[0])
+                except ValueError:
+                    continue
+                if idx != self.gpu:
+                    continue
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def ncu_traffic():
+    """DRAM bytes per walk launch from the committed ncu summary, scaled per body."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "walk_traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def accuracy_vs_direct(w, pm, acc, orc, nthreads, ntarget=1024):
+    """Median / p99 relative error of the step-0 accelerations against the FP64 direct sum on a
+    seeded subsample (the benchmark spec's <= 1e-3 gate)."""
+    from oracle.oracle import relerr
+
+    rng = np.random.default_rng(1234)
+    tgt = np.sort(rng.choice(len(pm), min(ntarget, len(pm)), replace=False)).astype(np.uint32)
+    pos = pm[:, :3].astype(np.float64)
+    mass = pm[:, 3].astype(np.float64)
+    d = orc.direct(pos, mass, w["eps"], targets=tgt, nthreads=nthreads)
+    err = relerr(acc[tgt], d)
+    return {"median_rel_err_vs_direct_fp64": float(np.median(err)), "p99": float(np.percentile(err, 99)),
+            "targets": int(len(tgt))}
+
+
+def cpu_sample(bh, w, pm, nthreads, walk_sample):
+    """Oracle port of one reference step on a bounded sample: bounds, keys, sort, kick+drift and
+    the tree build run on all N bodies; the walk runs on a seeded subsample and is scaled to N."""
+    from oracle.oracle import Restatement
+
+    orc = Restatement()
+    n = len(pm)
+    pos = pm[:, :3].astype(np.float64)
+    mass = pm[:, 3].astype(np.float64)
+    t0 = time.perf_counter()
+    c, size = orc.bounds(pos)
+    keys = orc.morton_keys(pos, size)
+    perm = orc.sort_perm(keys)
+    sp, sm = pos[perm], mass[perm]
+    t1 = time.perf_counter()
+    rng = np.random.default_rng(99)
+    tgt = np.sort(rng.choice(n, min(walk_sample, n), replace=False)).astype(np.uint32)
+    build_s, walk_s, _ = orc.time_sample(sp, sm, c, size * w["edge"], w["leaf"], 1, w["theta"], w["eps"], tgt,
+                                         nthreads=nthreads)
+    fixed = (t1 - t0) + build_s
+    per_step = fixed + walk_s * n / len(tgt)
+    return {"value": n / per_step, "unit": "body-steps/s", "cores": nthreads, "kind": "port",
+            "sample": (f"bounds+keys+sort on all {n} bodies ({t1 - t0:.2f} s) + tree build on all {n} "
+                       f"({build_s:.2f} s) + walk of {len(tgt)} sampled bodies ({walk_s:.2f} s) scaled to {n}; "
+                       f"{nthreads} thread(s); extrapolated step {per_step:.1f} s"),
+            "seconds_per_step": per_step}
+
+
+def run_reference(args, w, dist):
+    """CPU reference arm: the oracle port of the reference's step with all host threads."""
+    if dist.rank != 0:
+        return
+    import __graft_entry__
+
+    bh = __graft_entry__.package()
+    pm, _ = make_inputs(bh, w, w["seed"])
+    nthreads = os.cpu_count() or 1
+    sample = 65536
+    for _ in range(args.warmup):
+        pass  # a CPU step has no warm-up state; warm-up steps are not repeated
+    vals = []
+    t_all = time.perf_counter()
+    for k in range(args.steps):
+        r = cpu_sample(bh, w, pm, nthreads, sample)
+        vals.append(r["seconds_per_step"])
+    wall = time.perf_counter() - t_all
+    per_step = statistics.mean(vals)
+    value = w["n"] / per_step
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "bodies": w["n"], "desc": w["desc"]},
+            "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": nthreads, "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, w, dist):
+    import __graft_entry__
+
+    bh = __graft_entry__.package()
+    bh.load()
+    n = w["n"]
+    pm, vel = make_inputs(bh, w, w["seed"] + dist.rank)
+    prm = bh.default_params(theta=w["theta"], eps=w["eps"], dt=w["dt"], leaf_capacity=w["leaf"],
+                            multipole=bh.BH_MULTIPOLE_QUADRUPOLE, edge_factor=w["edge"], acc_follows_body=1)
+    sim = bh.Simulation(n, device=0)
+    sim.set_bodies(pm, vel)
+
+    # step-0 accelerations for the accuracy gate (rank 0, before stepping)
+    accuracy = None
+    if dist.rank == 0 and not args.no_accuracy:
+        from oracle.oracle import Restatement
+
+        c, size = sim.bounds()
+        sim.build(c, size * w["edge"], w["leaf"], bh.BH_MULTIPOLE_QUADRUPOLE)
+        acc0 = sim.force(w["theta"], w["eps"])
+        accuracy = accuracy_vs_direct(w, pm, acc0, Restatement(), os.cpu_count() or 1)
+        sim.set_bodies(pm, vel)
+
+    fp32_peak = sim.fp32_peak_tflops()
+    for _ in range(args.warmup):
+        sim.step(prm, 1, stats=False)
+    sim.synchronize()
+
+    gpu_index = int(os.environ.get("BH_GPU_INDEX", "0"))
+    per_step_ms, walk_ms, sort_ms, flops, inter = [], [], [], [], []
+    stage = {}
+    launches = 0
+    dist.barrier()
+    sim.synchronize()
+    with ClockSampler(gpu_index) as clocks:
+        t_wall = time.perf_counter()
+        for k in range(args.steps):
+            sim.flush_l2()
+            st = sim.step(prm, 1, stats=True)
+            per_step_ms.append(st.ms_step)
+            walk_ms.append(st.ms_walk)
+            sort_ms.append(st.ms_sort)
+            flops.append(FLOPS_P2P * st.interactions_p2p + FLOPS_CELL_QUAD * st.interactions_cell)
+            inter.append(st.interactions_p2p + st.interactions_cell)
+            launches += st.kernel_launches
+            for key, val in st.as_dict().items():
+                if key.startswith("ms_"):
+                    stage[key] = stage.get(key, 0.0) + val
+        sim.synchronize()
+        wall = time.perf_counter() - t_wall
+    dist.barrier()
+    total_ms = dist.max(sum(per_step_ms))
+    bodies_all = dist.sum(n * args.steps)
+    value = bodies_all / (total_ms * 1e-3)
+
+    # end to end through the C ABI with host buffers (pinned), one step per sample
+    e2e_ms = []
+    pin_p = bh.PinnedArray((n, 4))
+    pin_v = bh.PinnedArray((n, 4))
+    pin_p.array[:] = pm
+    pin_v.array[:] = vel
+    out_p = bh.PinnedArray((n, 4))
+    out_v = bh.PinnedArray((n, 4))
+    lib = bh.load()
+    for k in range(max(3, min(args.steps, 10))):
+        sim.flush_l2()
+        sim.event_record(0)
+        bh.check(lib.bh_set_bodies(sim.h, pin_p.array.ctypes.data, pin_v.array.ctypes.data, n), "set")
+        bh.check(lib.bh_step(sim.h, prm, 1, None), "step")
+        bh.check(lib.bh_get_bodies(sim.h, out_p.array.ctypes.data, out_v.array.ctypes.data, None), "get")
+        sim.event_record(1)
+        e2e_ms.append(sim.event_elapsed_ms(0, 1))
+    e2e_value = dist.sum(n) / (dist.max(statistics.median(e2e_ms)) * 1e-3)
+    for a in (pin_p, pin_v, out_p, out_v):
+        a.free()
+
+    mean_walk = statistics.mean(walk_ms)
+    walk_flops = statistics.mean(flops)
+    achieved_tflops = walk_flops / (mean_walk * 1e-3) / 1e12
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs")
+    sort_bytes = n * (8 + 24 * SORT_PASSES)
+    sort_gbs = sort_bytes / (statistics.mean(sort_ms) * 1e-3) / 1e9
+    traffic = ncu_traffic()
+    walk_traffic = None
+    if traffic and traffic.get("bytes_per_body"):
+        walk_traffic = traffic["bytes_per_body"] * n
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (keys, bounds, tree geometry and upsweep in f64)",
+        "data": "synthetic", "impl": "ours",
+        "config": {"workload": args.workload, "bodies": n, "desc": w["desc"],
+                   "timing": "per-step CUDA events on the library stream; L2 flushed between steps",
+                   "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"},
+        "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
+                "ms_per_step": statistics.median(e2e_ms)},
+        "interactions_per_s": dist.sum(sum(inter)) / (total_ms * 1e-3),
+        "interactions_per_body": statistics.mean(inter) / n,
+        "roofline": {"kernel": "k_walk<quadrupole>", "bound": "fp32", "achieved": achieved_tflops,
+                     "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved_tflops / fp32_peak,
+                     "peak_source": "measured FP32 FMA peak of this GPU (bh_measure_fp32_peak)",
+                     "traffic": walk_traffic,
+                     "flops_per_launch": walk_flops, "ms_per_launch": mean_walk},
+        "roofline_sort": {"kernel": "onesweep radix sort (Morton keys)", "bound": "hbm", "achieved": sort_gbs,
+                          "peak": hbm_peak, "unit": "GB/s",
+                          "frac": (sort_gbs / hbm_peak) if hbm_peak else None,
+                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                          "bytes_per_launch": sort_bytes},
+        "stage_ms_per_step": {k[3:]: v / args.steps for k, v in stage.items()},
+        "gpu_launches": launches,
+        "wall_s_timed_loop": wall,
+        "accuracy": accuracy,
+    }
+    if dist.rank == 0:
+        clk = clocks.summary()
+        line["clocks"] = clk
+        if dist.ws == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_sample(bh, w, pm, 1, args.cpu_walk_sample)
+            line["cpu_baseline"].pop("seconds_per_step", None)
+        print(json.dumps(line), flush=True)
+    sim.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="plummer-4m", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--cpu-walk-sample", type=int, default=16384)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warning: fewer than 3 warm-up steps")
+    w = WORKLOADS[args.workload]
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, w, dist)
+    else:
+        run_ours(args, w, dist)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,213 @@
+/*
+ * libbhgpu — GB300-native (sm_103a) per-step Barnes-Hut pipeline behind a C ABI.
+ *
+ * The entry points replace the per-step path of DavidRichardson02's "Serial Hashed-Octree
+ * Barnes-Hut N-Body Simulator 0_3" (paths below are relative to that project's root):
+ *
+ *   bh_compute_bounds   OctantBounds::OctantBounds(Body*, size_t)          src/OctantUtils.cpp:27-59
+ *   bh_morton_keys      computeMortonKey + interleaveBits                  src/MortonKeys.hpp:95-181
+ *   bh_sort_bodies      RadixSortBodies (ThreePassRadixSortMortonKeys,
+ *                       ReorderBodiesByIndexes)                            src/Body.hpp:257-302
+ *   bh_build            buildLinearHashedOctreeInPlace (insertBody,
+ *                       pruneEmptyNodes, computeTreeBaryCenters)           src/HashedOctree.hpp:211-244
+ *   bh_node_lookup      LinearHashedOctree::lookUpNode                     src/HashedOctree.cpp:111-115
+ *   bh_force            ResetVec3D + ComputeHOTOctreeForce
+ *                       (TraverseHOTInteractionList,
+ *                       ComputeHOTForceInteractionList, MAC)               src/HashedOctree.hpp:262-459
+ *   bh_kick_drift       ComputePositionAtHalfTimeStep                      src/Body.hpp:306-313
+ *   bh_kick             ComputeVelocityAndPosition                         src/Body.hpp:317-324
+ *   bh_step             one frame of ofApp::update + ofApp::draw
+ *                       (drawing excluded)                                 src/ofApp.cpp:169-177, 248-282
+ *   bh_set_bodies_ref / bh_get_bodies_ref
+ *                       the reference's 80-byte Body array (Body.hpp:30-65) <-> device state
+ *
+ * Conventions
+ *   - Every call returns a bh_status; no exception crosses the ABI.
+ *   - Host buffers belong to the caller; device buffers belong to the context and are reused
+ *     across steps. A context serves one host thread at a time.
+ *   - Device state is structure-of-arrays FP32: position+mass (x, y, z, m) and velocity
+ *     (vx, vy, vz, 0) as float4 per body, plus accelerations (ax, ay, az, 0). Bounds and keys
+ *     are computed in FP64 exactly as the reference does, so Morton keys, the sort
+ *     permutation and the octree node-key set are bit-identical to the reference's on the
+ *     same FP32 positions.
+ *   - The body order inside a context is the order of the last bh_sort_bodies / bh_step
+ *     (Morton order), as in the reference after RadixSortBodies.
+ *   - All work runs on one GPU, on the context's own CUDA stream. Calls that return data to
+ *     the host synchronise that stream.
+ */
+#ifndef BHGPU_H
+#define BHGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bh_status {
+  BH_OK = 0,
+  BH_ERR_INVALID_ARG = 1,     /* null pointer, n above capacity, bad parameter */
+  BH_ERR_OOM = 2,             /* device or pinned-host allocation failed */
+  BH_ERR_DEVICE = 3,          /* a CUDA runtime call failed (no GPU, launch failure, ...) */
+  BH_ERR_OVERFLOW_STACK = 4,  /* tree-walk stack overflow (device flag) */
+  BH_ERR_OVERFLOW_HASH = 5,   /* node hash table probe limit reached (device flag) */
+  BH_ERR_OVERFLOW_NODES = 6,  /* node arena too small; bh_step grows it and retries itself */
+  BH_ERR_TIMEOUT = 7,         /* a bounded device-side wait gave up (device flag) */
+  BH_ERR_NO_TREE = 8,         /* bh_force / bh_tree_* called before bh_build */
+  BH_ERR_NOT_FOUND = 9        /* bh_node_lookup: no node with that key */
+} bh_status;
+
+typedef enum bh_multipole_mode {
+  /* What the reference computes today: its upsweep never runs, so every node keeps the
+   * position of the first body inserted into it (insertion order = sorted order) as its
+   * barycentre, the running mass sum, and a zero quadrupole (src/HashedOctree.cpp:487,597,831). */
+  BH_MULTIPOLE_LITERAL = 0,
+  /* The reference's intended upsweep (src/HashedOctree.cpp:721-855): centre of mass and
+   * traceless quadrupole, accumulated bottom-up in FP64, used by the walk in FP32. */
+  BH_MULTIPOLE_QUADRUPOLE = 1
+} bh_multipole_mode;
+
+typedef struct bh_ctx bh_ctx;
+
+/* OctantBounds: centre = mean position; size = max_i,a (|p_ia| - c_a), the value the
+ * reference uses both as the Morton half-extent and as the root node's edge. */
+typedef struct bh_bounds {
+  double center[3];
+  double size;
+} bh_bounds;
+
+typedef struct bh_params {
+  double theta;          /* opening angle of the MAC size^2 / d^2 < theta^2 */
+  double eps;            /* Plummer softening (the reference hard-codes 0.025) */
+  double dt;             /* time step of the kick-drift-kick leapfrog */
+  int leaf_capacity;     /* bodies per leaf before it splits (the reference: 1) */
+  int multipole;         /* bh_multipole_mode */
+  double edge_factor;    /* root edge = edge_factor * bounds.size (the reference app: 1) */
+  int acc_follows_body;  /* 1: the first half-kick uses each body's own acceleration.
+                            0: the reference app's order, whose sort reorders bodies but not
+                            its acceleration array (src/ofApp.cpp:176,248). */
+} bh_params;
+
+/* Per-call statistics. Stage times are CUDA-event milliseconds summed over the steps of the
+ * call (filled when bh_step / bh_force get a non-null stats pointer). */
+typedef struct bh_stats {
+  double ms_step;          /* whole steps, first to last kernel */
+  double ms_bounds;
+  double ms_morton;
+  double ms_sort;          /* Morton-key sort of the bodies */
+  double ms_kick_drift;    /* gather into sorted order + first half-kick + drift + tree keys */
+  double ms_sort_tree;     /* tree-key sort */
+  double ms_build;         /* node discovery + hash table */
+  double ms_upsweep;
+  double ms_walk;          /* tree walk + force (+ second half-kick inside bh_step) */
+  uint64_t n_nodes;
+  uint64_t n_leaves;
+  uint64_t interactions_cell;  /* per-body counts, summed: accepted multi-body cells */
+  uint64_t interactions_p2p;   /* per-body counts, summed: single-body interactions */
+  uint32_t max_depth;
+  uint32_t error_flags;        /* device error word (bit set = BH_ERR_* code - 3) */
+  uint32_t steps;
+  uint32_t retries;            /* node-arena growths performed by bh_step */
+  uint32_t kernel_launches;    /* libbhgpu kernels launched by the call */
+} bh_stats;
+
+typedef struct bh_node {
+  uint64_t key;
+  int64_t count;       /* bodies at or below the node (HOTNode::N) */
+  double mass;
+  double com[3];       /* barycentre used by the walk (see bh_multipole_mode) */
+  double quad[6];      /* Qxx, Qxy, Qxz, Qyy, Qyz, Qzz */
+  double center[3];    /* node bounds */
+  double size;         /* node edge */
+  int32_t depth;
+  uint8_t child_byte;  /* bit o set = child in octant o exists (HOTNode::childByte) */
+} bh_node;
+
+const char* bh_status_string(bh_status s);
+
+/* Context with room for `capacity` bodies on CUDA device `device`. */
+bh_status bh_create(bh_ctx** out, size_t capacity, int device);
+bh_status bh_destroy(bh_ctx* ctx);
+
+/* Host <-> device state. pos_m4: n x (x, y, z, m); vel4: n x (vx, vy, vz, w). The physics
+ * ignores w, but it travels with its body through every reordering, so a caller can keep a
+ * body id there. bh_set_bodies zeroes the accelerations; bh_set_state sets them. */
+bh_status bh_set_bodies(bh_ctx* ctx, const float* pos_m4, const float* vel4, size_t n);
+bh_status bh_set_state(bh_ctx* ctx, const float* pos_m4, const float* vel4, const float* acc4, size_t n);
+bh_status bh_get_bodies(bh_ctx* ctx, float* pos_m4, float* vel4, float* acc4);
+bh_status bh_num_bodies(const bh_ctx* ctx, size_t* n);
+
+/* The reference's Body layout (80 bytes: ofColor@0, displayRadius@8, position@16,
+ * velocity@40, mass@64, bodyKey@72; FP64 vectors). Positions, velocities and masses are
+ * rounded to FP32 on upload; on download the other fields are left untouched and bodyKey is
+ * the last computed Morton key. */
+bh_status bh_set_bodies_ref(bh_ctx* ctx, const void* bodies, size_t n);
+bh_status bh_get_bodies_ref(bh_ctx* ctx, void* bodies, size_t n);
+
+/* OctantBounds(Body*, N) of the current positions. */
+bh_status bh_compute_bounds(bh_ctx* ctx, bh_bounds* out);
+
+/* computeMortonKey(position, size) for every body; the keys stay in the context (the
+ * reference stores them in Body::bodyKey) and are copied to keys_out when it is not null. */
+bh_status bh_morton_keys(bh_ctx* ctx, double size, uint64_t* keys_out);
+
+/* RadixSortBodies: stable sort of the bodies by their current keys. perm_out (optional)
+ * receives, per new slot, the previous slot of the body. Like the reference, the
+ * acceleration array is not reordered. */
+bh_status bh_sort_bodies(bh_ctx* ctx, uint32_t* perm_out);
+
+/* buildLinearHashedOctreeInPlace over the current bodies with the root cube
+ * (center, edge): node keys by prefix truncation of the bodies' depth-21 octant paths, an
+ * open-addressed device hash table over node keys, and the multipole pass of `multipole`.
+ * Leaves hold up to leaf_capacity bodies; a depth-21 leaf holds any number. */
+bh_status bh_build(bh_ctx* ctx, const double center[3], double edge, int leaf_capacity, int multipole);
+bh_status bh_tree_size(bh_ctx* ctx, size_t* n_nodes);
+/* All nodes sorted by key. Any output pointer may be null. Fails if cap < node count. */
+bh_status bh_tree_nodes(bh_ctx* ctx, size_t cap, uint64_t* keys, int64_t* counts, double* mass, double* com3,
+                        uint8_t* child_byte, double* quad6);
+bh_status bh_node_lookup(bh_ctx* ctx, uint64_t key, bh_node* out);
+
+/* ResetVec3D + ComputeHOTOctreeForce on the built tree: accelerations of every body,
+ * written into the context and, when acc4_out is not null, copied out (n x 4 floats). */
+bh_status bh_force(bh_ctx* ctx, double theta, double eps, float* acc4_out, bh_stats* stats);
+
+/* Leapfrog halves, using the context's accelerations slot by slot. */
+bh_status bh_kick_drift(bh_ctx* ctx, double dt);
+bh_status bh_kick(bh_ctx* ctx, double dt);
+
+/* nsteps frames of the reference's per-step sequence: bounds -> Morton keys -> sort ->
+ * kick+drift -> build (bounds of the pre-drift positions, edge = edge_factor * size) ->
+ * force -> kick. stats (optional) is filled for the call. */
+bh_status bh_step(bh_ctx* ctx, const bh_params* params, int nsteps, bh_stats* stats);
+
+/* Default parameters: theta 0.5, eps 0.025, dt 1e-3, leaf 1, quadrupole, edge 2, acc follows body. */
+void bh_params_default(bh_params* p);
+
+bh_status bh_synchronize(bh_ctx* ctx);
+
+/* CUDA events on the context's stream, for timing from the caller (slots 0..63). */
+bh_status bh_event_record(bh_ctx* ctx, int slot);
+bh_status bh_event_elapsed_ms(bh_ctx* ctx, int slot_start, int slot_end, float* ms);
+/* Writes a device buffer larger than the L2 cache on the context's stream. */
+bh_status bh_flush_l2(bh_ctx* ctx);
+
+/* Pinned host memory for fast transfers. */
+bh_status bh_host_alloc(void** ptr, size_t bytes);
+bh_status bh_host_free(void* ptr);
+
+/* Measured FP32 FMA throughput of this GPU (TFLOP/s, FMA = 2 flops), from a register-only
+ * kernel timed with CUDA events on the context's stream. */
+bh_status bh_measure_fp32_peak(bh_ctx* ctx, double* tflops);
+
+/* Host-side synthetic initial conditions (set-up time, not the per-step path): a Plummer
+ * sphere of n bodies, scale radius a, total mass mtot, shifted to its centre-of-mass frame,
+ * then offset by pos_offset3 / vel_offset3 (either may be null). */
+bh_status bh_plummer(uint64_t seed, size_t n, double a, double mtot, const double* pos_offset3,
+                     const double* vel_offset3, float* pos_m4, float* vel4);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BHGPU_H */

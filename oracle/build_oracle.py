@@ -1,0 +1,51 @@
+"""Builds the oracle libraries (test infrastructure only).
+
+    oracle/_build/liboracle.so  the CPU restatement (oracle/bh_oracle.cpp); built everywhere.
+    oracle/_ref/libbhref.so     REF-LITERAL: the reference's own hot-path translation units
+                                src/{MathUtils,Body,OctantUtils,HashedNode,HashedOctree}.cpp,
+                                compiled unmodified from the reference checkout (read in place,
+                                never copied) against oracle/ref_shim/ofMain.h, plus the C-ABI
+                                harness oracle/ref_harness.cpp. Built only where the reference
+                                checkout exists (REFERENCE_SRC, default /root/reference/src).
+
+Both use g++ -O2 -ffp-contract=off without -march flags, so no FMA contraction changes the
+FP64 results.
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SRC = os.environ.get("REFERENCE_SRC", "/root/reference/src")
+REF_TUS = ["MathUtils.cpp", "Body.cpp", "OctantUtils.cpp", "HashedNode.cpp", "HashedOctree.cpp"]
+FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread"]
+
+
+def build_restatement():
+    out_dir = os.path.join(HERE, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "liboracle.so")
+    subprocess.run(["g++", *FLAGS, "-o", out + ".tmp", os.path.join(HERE, "bh_oracle.cpp")], check=True)
+    os.replace(out + ".tmp", out)
+    return out
+
+
+def build_ref():
+    """Returns the library path, or None when the reference checkout is absent."""
+    if not all(os.path.exists(os.path.join(REF_SRC, f)) for f in REF_TUS):
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libbhref.so")
+    cmd = ["g++", *FLAGS, "-w", "-I" + os.path.join(HERE, "ref_shim"), "-I" + REF_SRC, "-o", out + ".tmp",
+           os.path.join(HERE, "ref_harness.cpp")] + [os.path.join(REF_SRC, f) for f in REF_TUS]
+    subprocess.run(cmd, check=True)
+    os.replace(out + ".tmp", out)
+    return out
+
+
+def build_all():
+    return build_restatement(), build_ref()
+
+
+if __name__ == "__main__":
+    print(build_all())

@@ -1,0 +1,314 @@
+"""ctypes binding of libbhgpu's C ABI (include/bhgpu.h), used by the tests and bench.py.
+
+The product is the C library; this module only loads it and converts numpy arrays. It never
+computes anything itself: if libbhgpu.so is missing or a call fails, it raises.
+
+Reference interface each method mirrors (paths relative to the reference project root):
+    Simulation.bounds()        OctantBounds::OctantBounds(Body*, size_t)   src/OctantUtils.cpp:27-59
+    Simulation.morton_keys()   computeMortonKey                            src/MortonKeys.hpp:137-181
+    Simulation.sort_bodies()   RadixSortBodies                             src/Body.hpp:275-302
+    Simulation.build()         buildLinearHashedOctreeInPlace              src/HashedOctree.hpp:211-244
+    Simulation.lookup()        LinearHashedOctree::lookUpNode              src/HashedOctree.cpp:111-115
+    Simulation.force()         ResetVec3D + ComputeHOTOctreeForce          src/HashedOctree.hpp:262-273
+    Simulation.kick_drift()    ComputePositionAtHalfTimeStep               src/Body.hpp:306-313
+    Simulation.kick()          ComputeVelocityAndPosition                  src/Body.hpp:317-324
+    Simulation.step()          ofApp::update + ofApp::draw per frame       src/ofApp.cpp:169-177, 248-282
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbhgpu.so")
+
+BH_MULTIPOLE_LITERAL = 0
+BH_MULTIPOLE_QUADRUPOLE = 1
+
+STATUS = {
+    0: "BH_OK", 1: "BH_ERR_INVALID_ARG", 2: "BH_ERR_OOM", 3: "BH_ERR_DEVICE", 4: "BH_ERR_OVERFLOW_STACK",
+    5: "BH_ERR_OVERFLOW_HASH", 6: "BH_ERR_OVERFLOW_NODES", 7: "BH_ERR_TIMEOUT", 8: "BH_ERR_NO_TREE",
+    9: "BH_ERR_NOT_FOUND",
+}
+
+EXPORTS = [
+    "bh_status_string", "bh_create", "bh_destroy", "bh_set_bodies", "bh_set_state", "bh_get_bodies",
+    "bh_num_bodies", "bh_set_bodies_ref", "bh_get_bodies_ref", "bh_compute_bounds", "bh_morton_keys",
+    "bh_sort_bodies", "bh_build", "bh_tree_size", "bh_tree_nodes", "bh_node_lookup", "bh_force",
+    "bh_kick_drift", "bh_kick", "bh_step", "bh_params_default", "bh_synchronize", "bh_event_record",
+    "bh_event_elapsed_ms", "bh_flush_l2", "bh_host_alloc", "bh_host_free", "bh_measure_fp32_peak",
+    "bh_plummer",
+]
+
+
+class BHError(RuntimeError):
+    def __init__(self, code, where):
+        self.code = code
+        super().__init__(f"{where}: {STATUS.get(code, code)}")
+
+
+class Bounds(ctypes.Structure):
+    _fields_ = [("center", ctypes.c_double * 3), ("size", ctypes.c_double)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("theta", ctypes.c_double), ("eps", ctypes.c_double), ("dt", ctypes.c_double),
+                ("leaf_capacity", ctypes.c_int), ("multipole", ctypes.c_int), ("edge_factor", ctypes.c_double),
+                ("acc_follows_body", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("ms_step", ctypes.c_double), ("ms_bounds", ctypes.c_double), ("ms_morton", ctypes.c_double),
+                ("ms_sort", ctypes.c_double), ("ms_kick_drift", ctypes.c_double), ("ms_sort_tree", ctypes.c_double),
+                ("ms_build", ctypes.c_double), ("ms_upsweep", ctypes.c_double), ("ms_walk", ctypes.c_double),
+                ("n_nodes", ctypes.c_uint64), ("n_leaves", ctypes.c_uint64),
+                ("interactions_cell", ctypes.c_uint64), ("interactions_p2p", ctypes.c_uint64),
+                ("max_depth", ctypes.c_uint32), ("error_flags", ctypes.c_uint32), ("steps", ctypes.c_uint32),
+                ("retries", ctypes.c_uint32), ("kernel_launches", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Node(ctypes.Structure):
+    _fields_ = [("key", ctypes.c_uint64), ("count", ctypes.c_int64), ("mass", ctypes.c_double),
+                ("com", ctypes.c_double * 3), ("quad", ctypes.c_double * 6), ("center", ctypes.c_double * 3),
+                ("size", ctypes.c_double), ("depth", ctypes.c_int32), ("child_byte", ctypes.c_uint8)]
+
+
+_lib = None
+
+
+def load():
+    """Loads libbhgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libbhgpu.so not built ({LIB_PATH}); run __graft_entry__.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    P, S, D, I = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double, ctypes.c_int
+    sig = {
+        "bh_status_string": ([I], ctypes.c_char_p),
+        "bh_create": ([ctypes.POINTER(P), S, I], I),
+        "bh_destroy": ([P], I),
+        "bh_set_bodies": ([P, P, P, S], I),
+        "bh_set_state": ([P, P, P, P, S], I),
+        "bh_get_bodies": ([P, P, P, P], I),
+        "bh_num_bodies": ([P, ctypes.POINTER(S)], I),
+        "bh_set_bodies_ref": ([P, P, S], I),
+        "bh_get_bodies_ref": ([P, P, S], I),
+        "bh_compute_bounds": ([P, ctypes.POINTER(Bounds)], I),
+        "bh_morton_keys": ([P, D, P], I),
+        "bh_sort_bodies": ([P, P], I),
+        "bh_build": ([P, P, D, I, I], I),
+        "bh_tree_size": ([P, ctypes.POINTER(S)], I),
+        "bh_tree_nodes": ([P, S, P, P, P, P, P, P], I),
+        "bh_node_lookup": ([P, ctypes.c_uint64, ctypes.POINTER(Node)], I),
+        "bh_force": ([P, D, D, P, ctypes.POINTER(Stats)], I),
+        "bh_kick_drift": ([P, D], I),
+        "bh_kick": ([P, D], I),
+        "bh_step": ([P, ctypes.POINTER(Params), I, ctypes.POINTER(Stats)], I),
+        "bh_params_default": ([ctypes.POINTER(Params)], None),
+        "bh_synchronize": ([P], I),
+        "bh_event_record": ([P, I], I),
+        "bh_event_elapsed_ms": ([P, I, I, ctypes.POINTER(ctypes.c_float)], I),
+        "bh_flush_l2": ([P], I),
+        "bh_host_alloc": ([ctypes.POINTER(P), S], I),
+        "bh_host_free": ([P], I),
+        "bh_measure_fp32_peak": ([P, ctypes.POINTER(D)], I),
+        "bh_plummer": ([ctypes.c_uint64, S, D, D, P, P, P, P], I),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def check(code, where):
+    if code != 0:
+        raise BHError(code, where)
+
+
+def plummer(seed, n, a=1.0, mtot=1.0, pos_offset=None, vel_offset=None):
+    """Plummer sphere (host generator of the library): returns (pos_m (n,4) f32, vel (n,4) f32)."""
+    lib = load()
+    pm = np.zeros((n, 4), np.float32)
+    v = np.zeros((n, 4), np.float32)
+    po = None if pos_offset is None else np.asarray(pos_offset, np.float64)
+    vo = None if vel_offset is None else np.asarray(vel_offset, np.float64)
+    check(lib.bh_plummer(seed, n, a, mtot, _ptr(po), _ptr(vo), _ptr(pm), _ptr(v)), "bh_plummer")
+    return pm, v
+
+
+def two_spheres(seed, n):
+    """Clustered workload: sphere A (n/2 bodies, a = 1, M = 1, at rest at the origin) and
+    sphere B (n/2 bodies, a = 0.1, M = 0.1, at (+10, 0, 0) moving with (-0.3, 0.1, 0))."""
+    na = n // 2
+    pa, va = plummer(seed, na, 1.0, 1.0)
+    pb, vb = plummer(seed + 1, n - na, 0.1, 0.1, (10.0, 0.0, 0.0), (-0.3, 0.1, 0.0))
+    return np.concatenate([pa, pb]), np.concatenate([va, vb])
+
+
+def default_params(**kw):
+    p = Params()
+    load().bh_params_default(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class Simulation:
+    """One libbhgpu context (one GPU, one stream)."""
+
+    def __init__(self, capacity, device=0):
+        lib = load()
+        self.lib = lib
+        h = ctypes.c_void_p()
+        check(lib.bh_create(ctypes.byref(h), capacity, device), "bh_create")
+        self.h = h
+        self.capacity = capacity
+
+    def close(self):
+        if self.h:
+            self.lib.bh_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n(self):
+        v = ctypes.c_size_t()
+        check(self.lib.bh_num_bodies(self.h, ctypes.byref(v)), "bh_num_bodies")
+        return v.value
+
+    def set_bodies(self, pos_m, vel, acc=None):
+        pos_m = np.ascontiguousarray(pos_m, np.float32)
+        vel = np.ascontiguousarray(vel, np.float32)
+        assert pos_m.shape[1] == 4 and vel.shape == pos_m.shape
+        if acc is not None:
+            acc = np.ascontiguousarray(acc, np.float32)
+            check(self.lib.bh_set_state(self.h, _ptr(pos_m), _ptr(vel), _ptr(acc), len(pos_m)), "bh_set_state")
+        else:
+            check(self.lib.bh_set_bodies(self.h, _ptr(pos_m), _ptr(vel), len(pos_m)), "bh_set_bodies")
+
+    def get_bodies(self):
+        n = self.n
+        p = np.zeros((n, 4), np.float32)
+        v = np.zeros((n, 4), np.float32)
+        a = np.zeros((n, 4), np.float32)
+        check(self.lib.bh_get_bodies(self.h, _ptr(p), _ptr(v), _ptr(a)), "bh_get_bodies")
+        return p, v, a
+
+    def bounds(self):
+        b = Bounds()
+        check(self.lib.bh_compute_bounds(self.h, ctypes.byref(b)), "bh_compute_bounds")
+        return np.array(b.center[:]), b.size
+
+    def morton_keys(self, size):
+        k = np.zeros(self.n, np.uint64)
+        check(self.lib.bh_morton_keys(self.h, size, _ptr(k)), "bh_morton_keys")
+        return k
+
+    def sort_bodies(self):
+        perm = np.zeros(self.n, np.uint32)
+        check(self.lib.bh_sort_bodies(self.h, _ptr(perm)), "bh_sort_bodies")
+        return perm
+
+    def build(self, center, edge, leaf_capacity=1, multipole=BH_MULTIPOLE_QUADRUPOLE):
+        c = np.ascontiguousarray(center, np.float64)
+        check(self.lib.bh_build(self.h, _ptr(c), edge, leaf_capacity, multipole), "bh_build")
+
+    def tree_size(self):
+        m = ctypes.c_size_t()
+        check(self.lib.bh_tree_size(self.h, ctypes.byref(m)), "bh_tree_size")
+        return m.value
+
+    def tree_nodes(self):
+        m = self.tree_size()
+        keys = np.zeros(m, np.uint64)
+        counts = np.zeros(m, np.int64)
+        mass = np.zeros(m)
+        com = np.zeros((m, 3))
+        cb = np.zeros(m, np.uint8)
+        q = np.zeros((m, 6))
+        check(self.lib.bh_tree_nodes(self.h, m, _ptr(keys), _ptr(counts), _ptr(mass), _ptr(com), _ptr(cb), _ptr(q)),
+              "bh_tree_nodes")
+        return dict(keys=keys, counts=counts, mass=mass, com=com, child_byte=cb, quad=q)
+
+    def lookup(self, key):
+        nd = Node()
+        check(self.lib.bh_node_lookup(self.h, int(key), ctypes.byref(nd)), "bh_node_lookup")
+        return nd
+
+    def force(self, theta, eps, stats=False):
+        a = np.zeros((self.n, 4), np.float32)
+        st = Stats()
+        check(self.lib.bh_force(self.h, theta, eps, _ptr(a), ctypes.byref(st)), "bh_force")
+        return (a, st) if stats else a
+
+    def kick_drift(self, dt):
+        check(self.lib.bh_kick_drift(self.h, dt), "bh_kick_drift")
+
+    def kick(self, dt):
+        check(self.lib.bh_kick(self.h, dt), "bh_kick")
+
+    def step(self, params, nsteps=1, stats=True):
+        st = Stats()
+        check(self.lib.bh_step(self.h, ctypes.byref(params), nsteps, ctypes.byref(st) if stats else None),
+              "bh_step")
+        return st
+
+    def synchronize(self):
+        check(self.lib.bh_synchronize(self.h), "bh_synchronize")
+
+    def event_record(self, slot):
+        check(self.lib.bh_event_record(self.h, slot), "bh_event_record")
+
+    def event_elapsed_ms(self, a, b):
+        ms = ctypes.c_float()
+        check(self.lib.bh_event_elapsed_ms(self.h, a, b, ctypes.byref(ms)), "bh_event_elapsed_ms")
+        return ms.value
+
+    def flush_l2(self):
+        check(self.lib.bh_flush_l2(self.h), "bh_flush_l2")
+
+    def fp32_peak_tflops(self):
+        v = ctypes.c_double()
+        check(self.lib.bh_measure_fp32_peak(self.h, ctypes.byref(v)), "bh_measure_fp32_peak")
+        return v.value
+
+
+class PinnedArray:
+    """numpy view of pinned host memory allocated by bh_host_alloc."""
+
+    def __init__(self, shape, dtype=np.float32):
+        self.lib = load()
+        nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        p = ctypes.c_void_p()
+        check(self.lib.bh_host_alloc(ctypes.byref(p), nbytes), "bh_host_alloc")
+        self.p = p
+        buf = (ctypes.c_char * nbytes).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self):
+        if self.p:
+            self.array = None
+            self.lib.bh_host_free(self.p)
+            self.p = None

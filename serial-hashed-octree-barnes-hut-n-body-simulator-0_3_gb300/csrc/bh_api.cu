@@ -1,0 +1,716 @@
+// The C ABI of include/bhgpu.h: context, state transfer, the per-stage entry points that
+// mirror the reference's calls, and the fused per-step driver.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "bh_internal.cuh"
+
+using bh::kLevels;
+
+namespace {
+
+constexpr size_t kMaxBodies = (1u << 30) - 1;  // sort look-back words hold 30-bit counts
+
+template <class T>
+bh_status dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  if (cudaMalloc((void**)p, sizeof(T) * count) != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return BH_ERR_OOM;
+  }
+  return BH_OK;
+}
+
+template <class T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+#define BH_TRY(expr)                     \
+  do {                                   \
+    bh_status s_ = (expr);               \
+    if (s_ != BH_OK) return s_;          \
+  } while (0)
+
+bh_status cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return BH_OK;
+  cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? BH_ERR_OOM : BH_ERR_DEVICE;
+}
+
+bh_status last_launch() { return cuda_status(cudaGetLastError()); }
+
+bh_status err_to_status(uint32_t e) {
+  for (int bit = 0; bit < 8; ++bit)
+    if (e & (1u << bit)) return (bh_status)(bit + 3);
+  return BH_OK;
+}
+
+__global__ void k_iota(uint32_t* v, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = (uint32_t)i;
+}
+
+bh_status ensure_nodes(bh_ctx* c, size_t need) {
+  if (c->node_cap >= need && c->nkey) return BH_OK;
+  size_t cap = std::max<size_t>(need, 1024);
+  dfree(c->nkey);
+  dfree(c->nrange);
+  dfree(c->wnode);
+  dfree(c->nf64);
+  dfree(c->nchildbyte);
+  dfree(c->hash_keys);
+  dfree(c->hash_vals);
+  c->hash_cap = 0;
+  c->hash_valid = false;
+  c->node_cap = 0;
+  BH_TRY(dalloc(&c->nkey, cap));
+  BH_TRY(dalloc(&c->nrange, cap));
+  BH_TRY(dalloc(&c->wnode, cap));
+  BH_TRY(dalloc(&c->nf64, cap));
+  BH_TRY(dalloc(&c->nchildbyte, cap));
+  c->node_cap = cap;
+  c->tree_valid = false;
+  return BH_OK;
+}
+
+bh_status ensure_hash(bh_ctx* c) {
+  size_t want = 1024;
+  while (want < 2 * c->node_cap) want <<= 1;
+  if (c->hash_cap >= want && c->hash_keys) return BH_OK;
+  dfree(c->hash_keys);
+  dfree(c->hash_vals);
+  c->hash_cap = 0;
+  BH_TRY(dalloc(&c->hash_keys, want));
+  BH_TRY(dalloc(&c->hash_vals, want));
+  c->hash_cap = want;
+  return BH_OK;
+}
+
+// Reads the device error word (and the counters) after finishing the stream.
+bh_status sync_and_check(bh_ctx* c, uint32_t* err_out = nullptr) {
+  cudaMemcpyAsync(c->h_err, c->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(c->h_counters, c->counters, sizeof(bh::Counters), cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(c->h_level_bounds, c->level_bounds, sizeof(int) * (kLevels + 2), cudaMemcpyDeviceToHost,
+                  c->stream);
+  BH_TRY(cuda_status(cudaStreamSynchronize(c->stream)));
+  if (err_out) *err_out = *c->h_err;
+  return BH_OK;
+}
+
+void clear_device_flags(bh_ctx* c) {
+  cudaMemsetAsync(c->err, 0, sizeof(uint32_t), c->stream);
+  cudaMemsetAsync(c->counters, 0, sizeof(bh::Counters), c->stream);
+}
+
+size_t initial_node_cap(size_t n) { return std::max<size_t>(2 * n + 64, 1024); }
+
+// Tree over the current bodies (slot order pos) with the tree geometry already in c->geom:
+// tree keys -> sort -> tree-order positions -> node discovery -> multipole pass.
+void enqueue_tree(bh_ctx* c, const float4* pos, int n, int leaf_cap, int mode, bool keys_ready) {
+  if (!keys_ready) bh::launch_treekey(c, pos, n, c->tkey, c->tslot);
+  uint64_t* ko;
+  uint32_t* vo;
+  bh::radix_sort_pairs(c, c->tkey, c->tslot, c->keys[1], c->vals[1], n, c->stream, &ko, &vo);
+  bh::launch_gather_tree(c, c->tslot, n, pos, c->tpos);
+}
+
+void record(bh_ctx* c, bh_stats* st, int k) {
+  if (st) cudaEventRecord(c->stage_ev[k], c->stream);
+}
+
+float elapsed(bh_ctx* c, int a, int b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->stage_ev[a], c->stage_ev[b]);
+  return ms;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bh_status_string(bh_status s) {
+  switch (s) {
+    case BH_OK: return "ok";
+    case BH_ERR_INVALID_ARG: return "invalid argument";
+    case BH_ERR_OOM: return "out of memory";
+    case BH_ERR_DEVICE: return "CUDA device error";
+    case BH_ERR_OVERFLOW_STACK: return "tree-walk stack overflow";
+    case BH_ERR_OVERFLOW_HASH: return "node hash table overflow";
+    case BH_ERR_OVERFLOW_NODES: return "node arena overflow";
+    case BH_ERR_TIMEOUT: return "device wait timed out";
+    case BH_ERR_NO_TREE: return "no tree has been built";
+    case BH_ERR_NOT_FOUND: return "node not found";
+  }
+  return "unknown status";
+}
+
+void bh_params_default(bh_params* p) {
+  if (!p) return;
+  p->theta = 0.5;
+  p->eps = 0.025;
+  p->dt = 1e-3;
+  p->leaf_capacity = 1;
+  p->multipole = BH_MULTIPOLE_QUADRUPOLE;
+  p->edge_factor = 2.0;
+  p->acc_follows_body = 1;
+}
+
+bh_status bh_destroy(bh_ctx* c) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : c->stage_ev)
+    if (e) cudaEventDestroy(e);
+  for (int k = 0; k < 2; ++k) {
+    dfree(c->pos[k]);
+    dfree(c->vel[k]);
+    dfree(c->keys[k]);
+    dfree(c->vals[k]);
+  }
+  dfree(c->acc);
+  dfree(c->body_key);
+  dfree(c->tkey);
+  dfree(c->tslot);
+  dfree(c->tpos);
+  dfree(c->sort.hist);
+  dfree(c->sort.lookback);
+  dfree(c->sort.tile_ctr);
+  dfree(c->nkey);
+  dfree(c->nrange);
+  dfree(c->wnode);
+  dfree(c->nf64);
+  dfree(c->nchildbyte);
+  dfree(c->lb_level);
+  dfree(c->level_bounds);
+  dfree(c->level_tile_ctr);
+  dfree(c->hash_keys);
+  dfree(c->hash_vals);
+  dfree(c->geom);
+  dfree(c->bounds_partial);
+  dfree(c->err);
+  dfree(c->counters);
+  if (c->flush_buf) cudaFree(c->flush_buf);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->h_counters) cudaFreeHost(c->h_counters);
+  if (c->h_level_bounds) cudaFreeHost(c->h_level_bounds);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return BH_OK;
+}
+
+bh_status bh_create(bh_ctx** out, size_t capacity, int device) {
+  if (!out || capacity == 0 || capacity > kMaxBodies) return BH_ERR_INVALID_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return BH_ERR_DEVICE;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return BH_ERR_DEVICE;
+  bh_ctx* c = new (std::nothrow) bh_ctx();
+  if (!c) return BH_ERR_OOM;
+  c->device = device;
+  c->cap = capacity;
+  auto fail = [&](bh_status s) {
+    bh_destroy(c);
+    return s;
+  };
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(BH_ERR_DEVICE);
+  for (auto& e : c->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return fail(BH_ERR_DEVICE);
+  for (auto& e : c->stage_ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return fail(BH_ERR_DEVICE);
+  bh_status s = BH_OK;
+  for (int k = 0; k < 2 && s == BH_OK; ++k) {
+    if ((s = dalloc(&c->pos[k], capacity)) != BH_OK) break;
+    if ((s = dalloc(&c->vel[k], capacity)) != BH_OK) break;
+    if ((s = dalloc(&c->keys[k], capacity)) != BH_OK) break;
+    s = dalloc(&c->vals[k], capacity);
+  }
+  if (s == BH_OK) s = dalloc(&c->acc, capacity);
+  if (s == BH_OK) s = dalloc(&c->body_key, capacity);
+  if (s == BH_OK) s = dalloc(&c->tkey, capacity);
+  if (s == BH_OK) s = dalloc(&c->tslot, capacity);
+  if (s == BH_OK) s = dalloc(&c->tpos, capacity);
+  c->sort.max_tiles = bh::sort_max_tiles(capacity);
+  if (s == BH_OK) s = dalloc(&c->sort.hist, 8 * 256);
+  if (s == BH_OK) s = dalloc(&c->sort.lookback, (size_t)8 * c->sort.max_tiles * 256);
+  if (s == BH_OK) s = dalloc(&c->sort.tile_ctr, 8);
+  c->lb_level_tiles = (int)((capacity + 255) / 256) + 1;
+  if (s == BH_OK) s = dalloc(&c->lb_level, (size_t)kLevels * c->lb_level_tiles);
+  if (s == BH_OK) s = dalloc(&c->level_bounds, kLevels + 2);
+  if (s == BH_OK) s = dalloc(&c->level_tile_ctr, kLevels);
+  if (s == BH_OK) s = dalloc(&c->geom, 1);
+  c->bounds_blocks = 152 * 2;
+  if (s == BH_OK) s = dalloc(&c->bounds_partial, (size_t)c->bounds_blocks * 6);
+  if (s == BH_OK) s = dalloc(&c->err, 1);
+  if (s == BH_OK) s = dalloc(&c->counters, 1);
+  if (s != BH_OK) return fail(s);
+  if (cudaMallocHost((void**)&c->h_err, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMallocHost((void**)&c->h_counters, sizeof(bh::Counters)) != cudaSuccess ||
+      cudaMallocHost((void**)&c->h_level_bounds, sizeof(int) * (kLevels + 2)) != cudaSuccess)
+    return fail(BH_ERR_OOM);
+  cudaMemsetAsync(c->err, 0, sizeof(uint32_t), c->stream);
+  cudaMemsetAsync(c->counters, 0, sizeof(bh::Counters), c->stream);
+  cudaMemsetAsync(c->acc, 0, sizeof(float4) * capacity, c->stream);
+  cudaMemsetAsync(c->body_key, 0, sizeof(uint64_t) * capacity, c->stream);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return fail(BH_ERR_DEVICE);
+  *out = c;
+  return BH_OK;
+}
+
+bh_status bh_num_bodies(const bh_ctx* c, size_t* n) {
+  if (!c || !n) return BH_ERR_INVALID_ARG;
+  *n = c->n;
+  return BH_OK;
+}
+
+bh_status bh_set_state(bh_ctx* c, const float* pos_m4, const float* vel4, const float* acc4, size_t n) {
+  if (!c || n > c->cap || (n > 0 && (!pos_m4 || !vel4))) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  c->n = n;
+  c->cur = 0;
+  c->tree_valid = false;
+  if (n > 0) {
+    cudaMemcpyAsync(c->pos[0], pos_m4, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->vel[0], vel4, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream);
+    if (acc4)
+      cudaMemcpyAsync(c->acc, acc4, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream);
+    else
+      cudaMemsetAsync(c->acc, 0, sizeof(float4) * n, c->stream);
+    cudaMemsetAsync(c->body_key, 0, sizeof(uint64_t) * n, c->stream);
+  }
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+bh_status bh_set_bodies(bh_ctx* c, const float* pos_m4, const float* vel4, size_t n) {
+  return bh_set_state(c, pos_m4, vel4, nullptr, n);
+}
+
+bh_status bh_get_bodies(bh_ctx* c, float* pos_m4, float* vel4, float* acc4) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  const size_t n = c->n;
+  if (n > 0) {
+    if (pos_m4) cudaMemcpyAsync(pos_m4, c->pos[c->cur], sizeof(float4) * n, cudaMemcpyDeviceToHost, c->stream);
+    if (vel4) cudaMemcpyAsync(vel4, c->vel[c->cur], sizeof(float4) * n, cudaMemcpyDeviceToHost, c->stream);
+    if (acc4) cudaMemcpyAsync(acc4, c->acc, sizeof(float4) * n, cudaMemcpyDeviceToHost, c->stream);
+  }
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+// Reference Body layout (80 bytes): ofColor@0, displayRadius@8, position@16, velocity@40,
+// mass@64, bodyKey@72.
+bh_status bh_set_bodies_ref(bh_ctx* c, const void* bodies, size_t n) {
+  if (!c || n > c->cap || (n > 0 && !bodies)) return BH_ERR_INVALID_ARG;
+  std::vector<float> p(4 * n), v(4 * n);
+  const unsigned char* b = (const unsigned char*)bodies;
+  for (size_t i = 0; i < n; ++i) {
+    double rec[8];
+    std::memcpy(rec, b + 80 * i + 16, 7 * sizeof(double));
+    for (int k = 0; k < 3; ++k) {
+      p[4 * i + k] = (float)rec[k];
+      v[4 * i + k] = (float)rec[3 + k];
+    }
+    p[4 * i + 3] = (float)rec[6];
+    v[4 * i + 3] = 0.f;
+  }
+  return bh_set_bodies(c, p.data(), v.data(), n);
+}
+
+bh_status bh_get_bodies_ref(bh_ctx* c, void* bodies, size_t n) {
+  if (!c || !bodies || n != c->n) return BH_ERR_INVALID_ARG;
+  std::vector<float> p(4 * n), v(4 * n);
+  std::vector<uint64_t> k(n);
+  BH_TRY(bh_get_bodies(c, p.data(), v.data(), nullptr));
+  if (n > 0) {
+    cudaMemcpy(k.data(), c->body_key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost);
+    BH_TRY(last_launch());
+  }
+  unsigned char* b = (unsigned char*)bodies;
+  for (size_t i = 0; i < n; ++i) {
+    double rec[7] = {p[4 * i], p[4 * i + 1], p[4 * i + 2], v[4 * i], v[4 * i + 1], v[4 * i + 2], p[4 * i + 3]};
+    std::memcpy(b + 80 * i + 16, rec, sizeof(rec));
+    std::memcpy(b + 80 * i + 72, &k[i], sizeof(uint64_t));
+  }
+  return BH_OK;
+}
+
+bh_status bh_compute_bounds(bh_ctx* c, bh_bounds* out) {
+  if (!c || !out) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  bh::launch_bounds(c, c->pos[c->cur], (int)c->n, 1.0);
+  BH_TRY(last_launch());
+  bh::Geom g;
+  cudaMemcpyAsync(&g, c->geom, sizeof(g), cudaMemcpyDeviceToHost, c->stream);
+  BH_TRY(cuda_status(cudaStreamSynchronize(c->stream)));
+  for (int a = 0; a < 3; ++a) out->center[a] = g.center[a];
+  out->size = g.size;
+  return BH_OK;
+}
+
+bh_status bh_morton_keys(bh_ctx* c, double size, uint64_t* keys_out) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  const int n = (int)c->n;
+  const double zero[3] = {0, 0, 0};
+  bh::launch_set_geom(c, zero, size, zero, 1.0);
+  bh::launch_morton(c, c->pos[c->cur], n, c->body_key, c->vals[0]);
+  BH_TRY(last_launch());
+  if (keys_out && n > 0)
+    cudaMemcpyAsync(keys_out, c->body_key, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, c->stream);
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+bh_status bh_sort_bodies(bh_ctx* c, uint32_t* perm_out) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  const int n = (int)c->n;
+  if (n == 0) return BH_OK;
+  clear_device_flags(c);
+  c->launches += 1;
+  k_iota<<<(n + 255) / 256, 256, 0, c->stream>>>(c->vals[0], n);
+  uint64_t* ko;
+  uint32_t* vo;
+  bh::radix_sort_pairs(c, c->body_key, c->vals[0], c->keys[1], c->vals[1], n, c->stream, &ko, &vo);
+  const int nx = 1 - c->cur;
+  bh::launch_gather(c, vo, n, c->pos[c->cur], c->vel[c->cur], c->pos[nx], c->vel[nx]);
+  BH_TRY(last_launch());
+  if (perm_out) cudaMemcpyAsync(perm_out, vo, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, c->stream);
+  uint32_t e = 0;
+  BH_TRY(sync_and_check(c, &e));
+  if (e) return err_to_status(e);
+  c->cur = nx;
+  c->tree_valid = false;
+  c->hash_valid = false;
+  return BH_OK;
+}
+
+bh_status bh_build(bh_ctx* c, const double center[3], double edge, int leaf_capacity, int multipole) {
+  if (!c || !center || !(edge > 0) || leaf_capacity < 1 ||
+      (multipole != BH_MULTIPOLE_LITERAL && multipole != BH_MULTIPOLE_QUADRUPOLE))
+    return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  const int n = (int)c->n;
+  BH_TRY(ensure_nodes(c, initial_node_cap(c->n)));
+  for (;;) {
+    clear_device_flags(c);
+    bh::launch_set_geom(c, center, edge, center, edge);
+    enqueue_tree(c, c->pos[c->cur], n, leaf_capacity, multipole, false);
+    bh::launch_build(c, n, leaf_capacity);
+    bh::launch_upsweep(c, n, leaf_capacity, multipole);
+    BH_TRY(last_launch());
+    uint32_t e = 0;
+    BH_TRY(sync_and_check(c, &e));
+    if (e & bh::kErrNodes) {
+      BH_TRY(ensure_nodes(c, c->node_cap * 2));
+      continue;
+    }
+    if (e) return err_to_status(e);
+    break;
+  }
+  c->tree_valid = true;
+  c->hash_valid = false;  // rebuilt on the first lookup after a build
+  c->tree_leaf_cap = leaf_capacity;
+  c->tree_mode = multipole;
+  for (int a = 0; a < 3; ++a) c->tree_center[a] = center[a];
+  c->tree_edge = edge;
+  return BH_OK;
+}
+
+bh_status bh_tree_size(bh_ctx* c, size_t* m) {
+  if (!c || !m) return BH_ERR_INVALID_ARG;
+  if (!c->tree_valid) return BH_ERR_NO_TREE;
+  *m = c->n ? (size_t)c->h_level_bounds[kLevels] : 0;
+  return BH_OK;
+}
+
+bh_status bh_tree_nodes(bh_ctx* c, size_t cap, uint64_t* keys, int64_t* counts, double* mass, double* com3,
+                        uint8_t* child_byte, double* quad6) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  if (!c->tree_valid) return BH_ERR_NO_TREE;
+  size_t m = 0;
+  BH_TRY(bh_tree_size(c, &m));
+  if (cap < m) return BH_ERR_INVALID_ARG;
+  if (m == 0) return BH_OK;
+  cudaSetDevice(c->device);
+  std::vector<int2> r(m);
+  std::vector<bh::NodeF64> f(m);
+  if (keys) cudaMemcpyAsync(keys, c->nkey, sizeof(uint64_t) * m, cudaMemcpyDeviceToHost, c->stream);
+  if (child_byte) cudaMemcpyAsync(child_byte, c->nchildbyte, m, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(r.data(), c->nrange, sizeof(int2) * m, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(f.data(), c->nf64, sizeof(bh::NodeF64) * m, cudaMemcpyDeviceToHost, c->stream);
+  BH_TRY(cuda_status(cudaStreamSynchronize(c->stream)));
+  for (size_t j = 0; j < m; ++j) {
+    if (counts) counts[j] = r[j].y;
+    if (mass) mass[j] = f[j].mass;
+    if (com3)
+      for (int a = 0; a < 3; ++a) com3[3 * j + a] = f[j].com[a];
+    if (quad6)
+      for (int k = 0; k < 6; ++k) quad6[6 * j + k] = f[j].q[k];
+  }
+  return BH_OK;
+}
+
+bh_status bh_node_lookup(bh_ctx* c, uint64_t key, bh_node* out) {
+  if (!c || !out) return BH_ERR_INVALID_ARG;
+  if (!c->tree_valid) return BH_ERR_NO_TREE;
+  cudaSetDevice(c->device);
+  if (!c->hash_valid) {
+    BH_TRY(ensure_hash(c));
+    clear_device_flags(c);
+    bh::launch_hash(c);
+    uint32_t e = 0;
+    BH_TRY(sync_and_check(c, &e));
+    if (e) return err_to_status(e);
+    c->hash_valid = true;
+  }
+  int* d_idx = nullptr;
+  BH_TRY(dalloc(&d_idx, 1));
+  bh::launch_lookup(c, key, d_idx);
+  int idx = -1;
+  cudaMemcpyAsync(&idx, d_idx, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  cudaStreamSynchronize(c->stream);
+  dfree(d_idx);
+  BH_TRY(last_launch());
+  if (idx < 0) return BH_ERR_NOT_FOUND;
+  int2 r;
+  bh::NodeF64 f;
+  uint8_t cb = 0;
+  cudaMemcpy(&r, c->nrange + idx, sizeof(r), cudaMemcpyDeviceToHost);
+  cudaMemcpy(&f, c->nf64 + idx, sizeof(f), cudaMemcpyDeviceToHost);
+  cudaMemcpy(&cb, c->nchildbyte + idx, 1, cudaMemcpyDeviceToHost);
+  BH_TRY(last_launch());
+  std::memset(out, 0, sizeof(*out));
+  out->key = key;
+  out->count = r.y;
+  out->mass = f.mass;
+  for (int a = 0; a < 3; ++a) out->com[a] = f.com[a];
+  for (int k = 0; k < 6; ++k) out->quad[k] = f.q[k];
+  out->child_byte = cb;
+  // node bounds from the key, by the reference's child-centre recurrence
+  int depth = 0;
+  for (uint64_t k = key; k > 1; k >>= 3) ++depth;
+  double cc[3] = {c->tree_center[0], c->tree_center[1], c->tree_center[2]}, s = c->tree_edge;
+  for (int d = depth - 1; d >= 0; --d) {
+    int o = (int)((key >> (3 * d)) & 7);
+    double half = s * 0.5;
+    for (int a = 0; a < 3; ++a) {
+      volatile double off = (((o >> (2 - a)) & 1) ? 0.5 : -0.5) * half;
+      cc[a] = cc[a] + off;
+    }
+    s = half;
+  }
+  for (int a = 0; a < 3; ++a) out->center[a] = cc[a];
+  out->size = s;
+  out->depth = depth;
+  return BH_OK;
+}
+
+bh_status bh_force(bh_ctx* c, double theta, double eps, float* acc4_out, bh_stats* st) {
+  if (!c || !(theta >= 0) || !(eps >= 0)) return BH_ERR_INVALID_ARG;
+  if (!c->tree_valid) return BH_ERR_NO_TREE;
+  cudaSetDevice(c->device);
+  const int n = (int)c->n;
+  clear_device_flags(c);
+  record(c, st, 0);
+  bh::launch_walk(c, n, (float)theta, (float)eps, c->tree_mode, c->acc, nullptr, 0.f);
+  record(c, st, 1);
+  BH_TRY(last_launch());
+  if (acc4_out && n > 0)
+    cudaMemcpyAsync(acc4_out, c->acc, sizeof(float4) * n, cudaMemcpyDeviceToHost, c->stream);
+  uint32_t e = 0;
+  BH_TRY(sync_and_check(c, &e));
+  if (st) {
+    std::memset(st, 0, sizeof(*st));
+    st->ms_walk = elapsed(c, 0, 1);
+    st->ms_step = st->ms_walk;
+    st->interactions_cell = c->h_counters->cell;
+    st->interactions_p2p = c->h_counters->p2p;
+    st->n_nodes = (uint64_t)c->h_level_bounds[kLevels];
+    st->error_flags = e;
+    st->kernel_launches = 1;
+  }
+  return err_to_status(e);
+}
+
+bh_status bh_kick_drift(bh_ctx* c, double dt) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  bh::launch_kick_drift(c, c->pos[c->cur], c->vel[c->cur], c->acc, (int)c->n, (float)dt, 1);
+  BH_TRY(last_launch());
+  c->tree_valid = false;
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+bh_status bh_kick(bh_ctx* c, double dt) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  bh::launch_kick_drift(c, c->pos[c->cur], c->vel[c->cur], c->acc, (int)c->n, (float)dt, 0);
+  BH_TRY(last_launch());
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+bh_status bh_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
+  if (!c || !prm || nsteps < 0 || prm->leaf_capacity < 1 || !(prm->theta >= 0) || !(prm->eps >= 0) ||
+      !(prm->edge_factor > 0) ||
+      (prm->multipole != BH_MULTIPOLE_LITERAL && prm->multipole != BH_MULTIPOLE_QUADRUPOLE))
+    return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  if (st) std::memset(st, 0, sizeof(*st));
+  const int n = (int)c->n;
+  if (n == 0 || nsteps == 0) return BH_OK;
+  BH_TRY(ensure_nodes(c, initial_node_cap(c->n)));
+  const float dt = (float)prm->dt;
+  const uint64_t launches0 = c->launches;
+  for (int s = 0; s < nsteps; ++s) {
+    uint32_t e = 0;
+    for (;;) {
+      const int nx = 1 - c->cur;
+      clear_device_flags(c);
+      record(c, st, 0);
+      bh::launch_bounds(c, c->pos[c->cur], n, prm->edge_factor);
+      record(c, st, 1);
+      bh::launch_morton(c, c->pos[c->cur], n, c->keys[0], c->vals[0]);
+      record(c, st, 2);
+      uint64_t* ko;
+      uint32_t* perm;
+      bh::radix_sort_pairs(c, c->keys[0], c->vals[0], c->keys[1], c->vals[1], n, c->stream, &ko, &perm);
+      record(c, st, 3);
+      bh::launch_gather_kd_treekey(c, perm, n, c->pos[c->cur], c->vel[c->cur], c->acc, prm->acc_follows_body, dt,
+                                   c->pos[nx], c->vel[nx], c->tkey, c->tslot);
+      record(c, st, 4);
+      enqueue_tree(c, c->pos[nx], n, prm->leaf_capacity, prm->multipole, true);
+      record(c, st, 5);
+      bh::launch_build(c, n, prm->leaf_capacity);
+      record(c, st, 6);
+      bh::launch_upsweep(c, n, prm->leaf_capacity, prm->multipole);
+      record(c, st, 7);
+      bh::launch_walk(c, n, (float)prm->theta, (float)prm->eps, prm->multipole, c->acc, c->vel[nx], 0.5f * dt);
+      record(c, st, 8);
+      BH_TRY(last_launch());
+      BH_TRY(sync_and_check(c, &e));
+      if (e & bh::kErrNodes) {
+        BH_TRY(ensure_nodes(c, c->node_cap * 2));
+        if (st) st->retries++;
+        continue;
+      }
+      break;
+    }
+    if (e) return err_to_status(e);
+    // the sorted Morton keys become the bodies' keys (Body::bodyKey after RadixSortBodies)
+    uint64_t* tmp = c->body_key;
+    c->body_key = c->keys[0];
+    c->keys[0] = tmp;
+    c->cur = 1 - c->cur;
+    c->tree_valid = true;
+    c->tree_leaf_cap = prm->leaf_capacity;
+    c->tree_mode = prm->multipole;
+    if (st) {
+      st->ms_step += elapsed(c, 0, 8);
+      st->ms_bounds += elapsed(c, 0, 1);
+      st->ms_morton += elapsed(c, 1, 2);
+      st->ms_sort += elapsed(c, 2, 3);
+      st->ms_kick_drift += elapsed(c, 3, 4);
+      st->ms_sort_tree += elapsed(c, 4, 5);
+      st->ms_build += elapsed(c, 5, 6);
+      st->ms_upsweep += elapsed(c, 6, 7);
+      st->ms_walk += elapsed(c, 7, 8);
+      st->n_nodes = (uint64_t)c->h_level_bounds[kLevels];
+      st->interactions_cell += c->h_counters->cell;
+      st->interactions_p2p += c->h_counters->p2p;
+      st->max_depth = std::max(st->max_depth, c->h_counters->max_depth);
+      st->steps++;
+    }
+  }
+  if (st) st->kernel_launches = (uint32_t)(c->launches - launches0);
+  // tree geometry of the last step, for node lookups
+  bh::Geom g;
+  cudaMemcpy(&g, c->geom, sizeof(g), cudaMemcpyDeviceToHost);
+  for (int a = 0; a < 3; ++a) c->tree_center[a] = g.tc[a];
+  c->tree_edge = g.tedge;
+  c->hash_valid = false;
+  return last_launch();
+}
+
+bh_status bh_synchronize(bh_ctx* c) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+bh_status bh_event_record(bh_ctx* c, int slot) {
+  if (!c || slot < 0 || slot >= bh::kNumEvents) return BH_ERR_INVALID_ARG;
+  return cuda_status(cudaEventRecord(c->ev[slot], c->stream));
+}
+
+bh_status bh_event_elapsed_ms(bh_ctx* c, int a, int b, float* ms) {
+  if (!c || !ms || a < 0 || b < 0 || a >= bh::kNumEvents || b >= bh::kNumEvents) return BH_ERR_INVALID_ARG;
+  BH_TRY(cuda_status(cudaEventSynchronize(c->ev[b])));
+  return cuda_status(cudaEventElapsedTime(ms, c->ev[a], c->ev[b]));
+}
+
+bh_status bh_flush_l2(bh_ctx* c) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  if (!c->flush_buf) {
+    c->flush_bytes = (size_t)512 << 20;
+    if (cudaMalloc(&c->flush_buf, c->flush_bytes) != cudaSuccess) {
+      cudaGetLastError();
+      c->flush_buf = nullptr;
+      return BH_ERR_OOM;
+    }
+  }
+  static int salt = 0;
+  return cuda_status(cudaMemsetAsync(c->flush_buf, (++salt) & 0xff, c->flush_bytes, c->stream));
+}
+
+bh_status bh_host_alloc(void** ptr, size_t bytes) {
+  if (!ptr) return BH_ERR_INVALID_ARG;
+  if (cudaMallocHost(ptr, bytes ? bytes : 1) != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return BH_ERR_OOM;
+  }
+  return BH_OK;
+}
+
+bh_status bh_host_free(void* ptr) {
+  if (ptr) cudaFreeHost(ptr);
+  return BH_OK;
+}
+
+bh_status bh_measure_fp32_peak(bh_ctx* c, double* tflops) {
+  if (!c || !tflops) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  float* sink = nullptr;
+  BH_TRY(dalloc(&sink, 1));
+  const int blocks = sms * 8;
+  bh::launch_fp32_peak(c->stream, sink, blocks);  // warm-up
+  cudaEventRecord(c->ev[bh::kNumEvents - 2], c->stream);
+  bh::launch_fp32_peak(c->stream, sink, blocks);
+  cudaEventRecord(c->ev[bh::kNumEvents - 1], c->stream);
+  float ms = 0;
+  cudaEventSynchronize(c->ev[bh::kNumEvents - 1]);
+  cudaEventElapsedTime(&ms, c->ev[bh::kNumEvents - 2], c->ev[bh::kNumEvents - 1]);
+  dfree(sink);
+  BH_TRY(last_launch());
+  const double flops = (double)blocks * 256 * 4096 * 16 * 8 * 2;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return BH_OK;
+}
+
+}  // extern "C"

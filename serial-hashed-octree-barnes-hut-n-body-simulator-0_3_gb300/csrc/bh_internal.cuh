@@ -1,0 +1,164 @@
+// Internal declarations shared by the libbhgpu translation units (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bhgpu.h"
+
+namespace bh {
+
+constexpr int kMaxDepth = 21;             // 21 bits per axis, 63-bit keys (reference: MortonKeys.hpp:42)
+constexpr int kLevels = kMaxDepth + 1;    // depths 0..21
+constexpr int kNumEvents = 64;
+
+// Device error word bits. bit = (bh_status code - 3), so the host maps them back.
+enum : uint32_t {
+  kErrStack = 1u << (BH_ERR_OVERFLOW_STACK - 3),
+  kErrHash = 1u << (BH_ERR_OVERFLOW_HASH - 3),
+  kErrNodes = 1u << (BH_ERR_OVERFLOW_NODES - 3),
+  kErrTimeout = 1u << (BH_ERR_TIMEOUT - 3),
+};
+
+// Geometry of one step, produced on the device by the bounds kernel (or set by the host
+// for caller-given bounds) and read by the key kernels.
+struct Geom {
+  double center[3];  // OctantBounds::center
+  double size;       // OctantBounds::size (S)
+  double frac;       // 2^21 / (2 S): Morton scale
+  double tc[3];      // tree root centre
+  double tedge;      // tree root edge
+  double tscale;     // 2^21 / tedge
+  double tmargin;    // fast-path margin in key units (see tree_key)
+};
+
+// Walk record of one node: 64 bytes, read by the tree walk.
+//   mac : centre of mass (x, y, z) and edge^2; edge^2 is stored negated for single-body
+//         leaves so the walk can route them to the point list without another load.
+//   mq  : mass, Qxx, Qxy, Qxz
+//   q2  : Qyy, Qyz, Qzz, unused
+//   link: first child, child count, first body (tree order), body count
+struct __align__(16) WalkNode {
+  float4 mac;
+  float4 mq;
+  float4 q2;
+  int4 link;
+};
+
+// FP64 multipole of one node, kept for the parents during the upsweep.
+struct __align__(16) NodeF64 {
+  double com[3];
+  double mass;
+  double q[6];
+  uint32_t min_rank;  // smallest Morton slot among members (literal barycentre)
+  uint32_t pad;
+};
+
+struct Counters {
+  unsigned long long cell;
+  unsigned long long p2p;
+  unsigned int group_next;  // walk work queue
+  unsigned int max_depth;
+};
+
+// Radix sort (onesweep) scratch.
+struct SortScratch {
+  uint32_t* hist = nullptr;        // [8][256] digit counts, then exclusive offsets
+  uint32_t* lookback = nullptr;    // [8][max_tiles][256]
+  uint32_t* tile_ctr = nullptr;    // [8]
+  int max_tiles = 0;
+};
+
+struct Arena {
+  void* base = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace bh
+
+struct bh_ctx {
+  int device = 0;
+  size_t cap = 0;  // bodies
+  size_t n = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[bh::kNumEvents] = {};
+  cudaEvent_t stage_ev[16] = {};
+
+  // body state (Morton order), ping-pong
+  float4* pos[2] = {nullptr, nullptr};
+  float4* vel[2] = {nullptr, nullptr};
+  float4* acc = nullptr;
+  int cur = 0;
+
+  // keys / sort
+  uint64_t* keys[2] = {nullptr, nullptr};
+  uint32_t* vals[2] = {nullptr, nullptr};
+  uint64_t* body_key = nullptr;  // last Morton keys, per slot
+  bh::SortScratch sort;
+
+  // tree (over the bodies in tree-key order)
+  uint64_t* tkey = nullptr;   // sorted tree keys
+  uint32_t* tslot = nullptr;  // tree order -> body slot
+  float4* tpos = nullptr;     // positions+mass in tree order
+  size_t node_cap = 0;
+  uint64_t* nkey = nullptr;
+  int2* nrange = nullptr;  // first body, body count
+  bh::WalkNode* wnode = nullptr;
+  bh::NodeF64* nf64 = nullptr;
+  uint8_t* nchildbyte = nullptr;
+  uint32_t* lb_level = nullptr;  // look-back words of the level build
+  int lb_level_tiles = 0;
+  int* level_bounds = nullptr;  // [kLevels + 1] node index where each depth starts
+  uint32_t* level_tile_ctr = nullptr;  // [kLevels]
+  uint64_t* hash_keys = nullptr;
+  int* hash_vals = nullptr;
+  size_t hash_cap = 0;
+  bool hash_valid = false;
+  bool tree_valid = false;
+  int tree_leaf_cap = 1;
+  int tree_mode = 1;
+  double tree_center[3] = {0, 0, 0};
+  double tree_edge = 0;
+
+  bh::Geom* geom = nullptr;  // device
+  double* bounds_partial = nullptr;
+  int bounds_blocks = 0;
+  uint32_t* err = nullptr;
+  bh::Counters* counters = nullptr;
+
+  // host mirror of small device results
+  uint32_t* h_err = nullptr;  // pinned
+  bh::Counters* h_counters = nullptr;
+  int* h_level_bounds = nullptr;
+
+  void* flush_buf = nullptr;
+  size_t flush_bytes = 0;
+  uint64_t launches = 0;  // kernels launched on this context (every launcher adds its count)
+};
+
+namespace bh {
+
+// Kernel launchers (defined in the .cu files; all asynchronous on `st`).
+void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t* keys_tmp, uint32_t* vals_tmp,
+                      int n, cudaStream_t st, uint64_t** keys_out, uint32_t** vals_out);
+int sort_max_tiles(size_t n);
+
+void launch_bounds(bh_ctx* c, const float4* pos, int n, double edge_factor);
+void launch_set_geom(bh_ctx* c, const double center[3], double size, const double tcenter[3], double tedge);
+void launch_morton(bh_ctx* c, const float4* pos, int n, uint64_t* keys, uint32_t* idx);
+void launch_gather(bh_ctx* c, const uint32_t* perm, int n, const float4* pin, const float4* vin, float4* pout,
+                   float4* vout);
+void launch_gather_kd_treekey(bh_ctx* c, const uint32_t* perm, int n, const float4* pin, const float4* vin,
+                              const float4* acc, int acc_follows_body, float dt, float4* pout, float4* vout,
+                              uint64_t* tkeys, uint32_t* tidx);
+void launch_treekey(bh_ctx* c, const float4* pos, int n, uint64_t* tkeys, uint32_t* tidx);
+void launch_kick_drift(bh_ctx* c, float4* pos, float4* vel, const float4* acc, int n, float dt, int drift);
+void launch_gather_tree(bh_ctx* c, const uint32_t* tslot, int n, const float4* pos, float4* tpos);
+void launch_build(bh_ctx* c, int n, int leaf_cap);
+void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode);
+void launch_hash(bh_ctx* c);
+void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc_slot, float4* vel_kick,
+                 float half_dt);
+void launch_lookup(bh_ctx* c, uint64_t key, int* out_index);
+void launch_fp32_peak(cudaStream_t st, float* sink, int blocks);
+
+}  // namespace bh

@@ -1,0 +1,270 @@
+// Stable LSD radix sort of (u64 key, u32 value) pairs: one histogram pass over all digits,
+// then one "onesweep" pass per 8-bit digit (Adinets & Merrill, 2022): each block ranks a
+// 4096-key tile with warp-match multisplit, publishes its digit counts, resolves its global
+// offsets with a decoupled look-back over the preceding tiles, stages the tile in shared
+// memory in digit order and writes every digit run contiguously.
+//
+// Replaces ThreePassRadixSortMortonKeys / RadixSortPass (src/MortonKeys.hpp:373-470): the
+// reference runs stable byte passes at shifts 0,8,16,21,29,37,42,50,58, which together are a
+// full stable sort by the 64-bit key; this sort produces the same permutation with passes at
+// shifts 0,8,...,56. Stability: within a tile keys are ranked in input order (warp-major,
+// then item, then lane, which is the load order), and tiles are ordered by the look-back.
+#include <cuda_runtime.h>
+
+#include "bh_internal.cuh"
+
+namespace bh {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr int kTile = kThreads * kItems;  // 4096 keys
+constexpr int kPasses = 8;
+constexpr int kRadix = 256;
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagPrefix = 2u << 30;
+constexpr uint32_t kValMask = (1u << 30) - 1;
+constexpr int kSpinLimit = 1 << 22;  // about a second of polling; then the sort reports a timeout
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Digit counts of all 8 passes in one read of the keys. Each thread walks a contiguous run of
+// keys and run-length-merges equal digits before touching shared memory: the keys arrive in
+// the previous step's sorted order, so the high digits come in long runs.
+__global__ __launch_bounds__(kThreads) void k_hist(const uint64_t* __restrict__ keys, int n,
+                                                   uint32_t* __restrict__ hist) {
+  __shared__ uint32_t sh[kPasses * kRadix];
+  for (int i = threadIdx.x; i < kPasses * kRadix; i += kThreads) sh[i] = 0;
+  __syncthreads();
+  constexpr int kRun = 8;
+  const long long stride = (long long)gridDim.x * kThreads * kRun;
+  for (long long base = ((long long)blockIdx.x * kThreads + threadIdx.x) * kRun; base < n; base += stride) {
+    uint32_t cur[kPasses], cnt[kPasses];
+#pragma unroll
+    for (int p = 0; p < kPasses; ++p) cnt[p] = 0, cur[p] = 0;
+#pragma unroll
+    for (int j = 0; j < kRun; ++j) {
+      long long i = base + j;
+      if (i < n) {
+        uint64_t k = keys[i];
+#pragma unroll
+        for (int p = 0; p < kPasses; ++p) {
+          uint32_t d = (uint32_t)(k >> (8 * p)) & 0xFFu;
+          if (cnt[p] && d != cur[p]) {
+            atomicAdd(&sh[p * kRadix + cur[p]], cnt[p]);
+            cnt[p] = 0;
+          }
+          cur[p] = d;
+          cnt[p] += 1;
+        }
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < kPasses; ++p)
+      if (cnt[p]) atomicAdd(&sh[p * kRadix + cur[p]], cnt[p]);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kPasses * kRadix; i += kThreads) {
+    uint32_t v = sh[i];
+    if (v) atomicAdd(&hist[i], v);
+  }
+}
+
+// Exclusive scan of each pass's 256 digit counts, in place. One block per pass.
+__global__ __launch_bounds__(kRadix) void k_hist_scan(uint32_t* __restrict__ hist) {
+  __shared__ uint32_t warp_tot[kRadix / 32];
+  uint32_t* h = hist + blockIdx.x * kRadix;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  uint32_t v = h[t], x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  uint32_t add = 0;
+  for (int i = 0; i < w; ++i) add += warp_tot[i];
+  h[t] = x - v + add;
+}
+
+struct OnesweepSmem {
+  uint64_t keys[kTile];
+  uint32_t vals[kTile];
+  uint32_t warp_cnt[kWarps][kRadix];
+  uint32_t digit_start[kRadix];
+  uint32_t global_base[kRadix];
+  uint32_t warp_tot[kWarps];
+  uint32_t tile;
+};
+
+__global__ __launch_bounds__(kThreads) void k_onesweep(const uint64_t* __restrict__ kin,
+                                                       const uint32_t* __restrict__ vin,
+                                                       uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                       int n, int shift, const uint32_t* __restrict__ digit_off,
+                                                       uint32_t* __restrict__ lookback,
+                                                       uint32_t* __restrict__ tile_ctr, uint32_t* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  OnesweepSmem& s = *reinterpret_cast<OnesweepSmem*>(smem_raw);
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+
+  if (t == 0) s.tile = atomicAdd(tile_ctr, 1u);
+  for (int i = t; i < kWarps * kRadix; i += kThreads) (&s.warp_cnt[0][0])[i] = 0;
+  __syncthreads();
+  const uint32_t tile = s.tile;
+  const long long base = (long long)tile * kTile;
+  const int valid_count = (int)min((long long)kTile, (long long)n - base);
+
+  uint64_t key[kItems];
+  uint32_t val[kItems];
+  uint32_t rank[kItems];
+  const long long wbase = base + (long long)w * (32 * kItems);
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    long long idx = wbase + j * 32 + lane;
+    bool ok = idx < n;
+    key[j] = ok ? kin[idx] : 0ull;
+    val[j] = ok ? vin[idx] : 0u;
+  }
+  const uint32_t lt_mask = (1u << lane) - 1u;
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    long long idx = wbase + j * 32 + lane;
+    bool ok = idx < n;
+    uint32_t d = (uint32_t)(key[j] >> shift) & 0xFFu;
+    uint32_t tag = ok ? d : (0x100u + (uint32_t)lane);  // invalid lanes never match
+    uint32_t peers = __match_any_sync(0xffffffffu, tag);
+    uint32_t pre = ok ? s.warp_cnt[w][d] : 0u;
+    __syncwarp();
+    if (ok && lane == __ffs(peers) - 1) s.warp_cnt[w][d] = pre + __popc(peers);
+    __syncwarp();
+    rank[j] = pre + __popc(peers & lt_mask);
+  }
+  __syncthreads();
+
+  // per-digit: warp-exclusive offsets and the tile total (thread t owns digit t)
+  uint32_t total = 0;
+#pragma unroll
+  for (int ww = 0; ww < kWarps; ++ww) {
+    uint32_t c = s.warp_cnt[ww][t];
+    s.warp_cnt[ww][t] = total;
+    total += c;
+  }
+  // publish this tile's aggregate (tile 0 publishes its inclusive prefix directly)
+  uint32_t* my_lb = lookback + (size_t)tile * kRadix + t;
+  st_relaxed(my_lb, (tile == 0 ? kFlagPrefix : kFlagAgg) | total);
+
+  // block-local exclusive scan over digits -> start of each digit run in the staged tile
+  uint32_t x = total;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s.warp_tot[w] = x;
+  __syncthreads();
+  uint32_t add = 0;
+  for (int i = 0; i < w; ++i) add += s.warp_tot[i];
+  s.digit_start[t] = x - total + add;
+  __syncthreads();
+
+  // stage the tile in digit order
+#pragma unroll
+  for (int j = 0; j < kItems; ++j) {
+    long long idx = wbase + j * 32 + lane;
+    if (idx < n) {
+      uint32_t d = (uint32_t)(key[j] >> shift) & 0xFFu;
+      uint32_t lp = s.digit_start[d] + s.warp_cnt[w][d] + rank[j];
+      s.keys[lp] = key[j];
+      s.vals[lp] = val[j];
+    }
+  }
+
+  // decoupled look-back for digit t
+  uint32_t excl = 0;
+  if (tile > 0) {
+    long long k = (long long)tile - 1;
+    int spins = 0;
+    while (k >= 0) {
+      uint32_t v = ld_relaxed(lookback + (size_t)k * kRadix + t);
+      uint32_t flag = v & ~kValMask;
+      if (flag == 0) {
+        if (++spins > kSpinLimit) {
+          atomicOr(err, kErrTimeout);
+          break;
+        }
+        __nanosleep(32);
+        continue;
+      }
+      excl += v & kValMask;
+      if (flag == kFlagPrefix) break;
+      --k;
+    }
+    st_relaxed(my_lb, kFlagPrefix | ((excl + total) & kValMask));
+  }
+  s.global_base[t] = digit_off[t] + excl;
+  __syncthreads();
+
+  for (int i = t; i < valid_count; i += kThreads) {
+    uint64_t kk = s.keys[i];
+    uint32_t d = (uint32_t)(kk >> shift) & 0xFFu;
+    uint32_t gp = s.global_base[d] + (uint32_t)i - s.digit_start[d];
+    if (gp < (uint32_t)n) {  // always true unless a look-back wait timed out (flagged above)
+      kout[gp] = kk;
+      vout[gp] = s.vals[i];
+    }
+  }
+}
+
+}  // namespace
+
+int sort_max_tiles(size_t n) { return (int)((n + kTile - 1) / kTile); }
+
+// Sorts (keys_in, vals_in) stably by the full 64-bit key. The result lands in keys_in /
+// vals_in (an even number of passes); the *_tmp buffers are scratch of the same size.
+void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t* keys_tmp, uint32_t* vals_tmp,
+                      int n, cudaStream_t st, uint64_t** keys_out, uint32_t** vals_out) {
+  *keys_out = keys_in;
+  *vals_out = vals_in;
+  if (n <= 1) return;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(OnesweepSmem));
+    attr_set = true;
+  }
+  const int tiles = sort_max_tiles((size_t)n);
+  cudaMemsetAsync(c->sort.hist, 0, sizeof(uint32_t) * kPasses * kRadix, st);
+  cudaMemsetAsync(c->sort.lookback, 0, sizeof(uint32_t) * (size_t)kPasses * tiles * kRadix, st);
+  cudaMemsetAsync(c->sort.tile_ctr, 0, sizeof(uint32_t) * kPasses, st);
+  int hblocks = (int)min((long long)152 * 4, ((long long)n + kThreads * 8 - 1) / (kThreads * 8));
+  c->launches += 2 + kPasses;
+  k_hist<<<hblocks, kThreads, 0, st>>>(keys_in, n, c->sort.hist);
+  k_hist_scan<<<kPasses, kRadix, 0, st>>>(c->sort.hist);
+  uint64_t* ka = keys_in;
+  uint32_t* va = vals_in;
+  uint64_t* kb = keys_tmp;
+  uint32_t* vb = vals_tmp;
+  for (int p = 0; p < kPasses; ++p) {
+    k_onesweep<<<tiles, kThreads, sizeof(OnesweepSmem), st>>>(ka, va, kb, vb, n, 8 * p, c->sort.hist + p * kRadix,
+                                                              c->sort.lookback + (size_t)p * tiles * kRadix,
+                                                              c->sort.tile_ctr + p, c->err);
+    uint64_t* tk = ka;
+    ka = kb;
+    kb = tk;
+    uint32_t* tv = va;
+    va = vb;
+    vb = tv;
+  }
+  *keys_out = ka;
+  *vals_out = va;
+}
+
+}  // namespace bh

@@ -1,0 +1,84 @@
+"""C ABI surface (no GPU needed): the library loads, exports every function include/bhgpu.h
+declares, refuses to run without a GPU, and its host-side generator is deterministic."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "bhgpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(bh_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_binding_list(bh):
+    assert header_functions() == sorted(bh.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(bh):
+    lib = bh.load()
+    out = subprocess.run(["nm", "-D", "--defined-only", bh.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (bh_\w+)", out))
+    for name in header_functions():
+        assert name in exported, name
+        assert getattr(lib, name) is not None
+
+
+def test_no_gpu_fails_loudly(bh):
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    lib = bh.load()
+    h = ctypes.c_void_p()
+    rc = lib.bh_create(ctypes.byref(h), 1024, 0)
+    assert rc == 3  # BH_ERR_DEVICE: no silent CPU path
+    with pytest.raises(bh.BHError):
+        bh.Simulation(1024)
+
+
+def test_invalid_arguments(bh):
+    lib = bh.load()
+    h = ctypes.c_void_p()
+    assert lib.bh_create(ctypes.byref(h), 0, 0) == 1
+    assert lib.bh_create(None, 10, 0) == 1
+    assert lib.bh_destroy(None) == 1
+    assert lib.bh_step(None, None, 1, None) == 1
+    assert lib.bh_status_string(6) == b"node arena overflow"
+
+
+def test_plummer_is_deterministic_and_centred(bh):
+    a, va = bh.plummer(42, 5000)
+    b, vb = bh.plummer(42, 5000)
+    c, _ = bh.plummer(43, 5000)
+    assert np.array_equal(a, b) and np.array_equal(va, vb)
+    assert not np.array_equal(a, c)
+    assert np.allclose(a[:, 3], 1.0 / 5000)
+    com = (a[:, :3].astype(np.float64)).mean(0)
+    assert np.all(np.abs(com) < 1e-6)
+    r = np.linalg.norm(a[:, :3], axis=1)
+    assert r.max() <= 10.0 + 1e-5
+    # Plummer: half-mass radius a / sqrt(2^(2/3) - 1) = 1.305
+    assert abs(np.median(r) - 1.305) < 0.05
+    # virial equilibrium: 2T/|W| ~ 1 (W = -3 pi M^2 / (32 a) for the Plummer model)
+    v = np.linalg.norm(va[:, :3], axis=1)
+    T = 0.5 * (a[:, 3] * v * v).sum()
+    assert abs(2 * T / (3 * np.pi / 32) - 1) < 0.05
+
+
+def test_two_spheres_layout(bh):
+    p, v = bh.two_spheres(9, 4000)
+    a, b = p[:2000], p[2000:]
+    assert np.allclose(a[:, :3].mean(0), 0, atol=1e-5)
+    assert np.allclose(b[:, :3].mean(0), (10, 0, 0), atol=1e-4)
+    assert np.isclose(b[:, 3].sum(), 0.1, rtol=1e-5) and np.isclose(a[:, 3].sum(), 1.0, rtol=1e-5)
+    assert np.allclose(v[2000:, :3].mean(0), (-0.3, 0.1, 0), atol=1e-5)
