@@ -279,7 +279,7 @@ def run_ours(args, w, dist):
     sim.synchronize()
 
     gpu_index = int(os.environ.get("BH_GPU_INDEX", "0"))
-    per_step_ms, walk_ms, sort_ms, flops, inter = [], [], [], [], []
+    per_step_ms, walk_ms, sort_ms, flops, inter, util_cell, util_pt = [], [], [], [], [], [], []
     stage = {}
     launches = 0
     dist.barrier()
@@ -294,6 +294,8 @@ def run_ours(args, w, dist):
             sort_ms.append(st.ms_sort)
             flops.append(FLOPS_P2P * st.interactions_p2p + FLOPS_CELL_QUAD * st.interactions_cell)
             inter.append(st.interactions_p2p + st.interactions_cell)
+            util_cell.append((st.interactions_cell, st.walk_cell_evals))
+            util_pt.append((st.interactions_p2p, st.walk_point_evals))
             launches += st.kernel_launches
             for key, val in st.as_dict().items():
                 if key.startswith("ms_"):
@@ -361,6 +363,10 @@ def run_ours(args, w, dist):
                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                           "bytes_per_launch": sort_bytes},
         "stage_ms_per_step": {k[3:]: v / args.steps for k, v in stage.items()},
+        "walk_lane_utilization": {
+            "cells": sum(a for a, _ in util_cell) / max(1, 32 * sum(b for _, b in util_cell)),
+            "points": sum(a for a, _ in util_pt) / max(1, 32 * sum(b for _, b in util_pt)),
+            "cell_share": sum(a for a, _ in util_cell) / max(1, sum(inter))},
         "gpu_launches": launches,
         "wall_s_timed_loop": wall,
         "accuracy": accuracy,

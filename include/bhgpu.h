@@ -110,6 +110,8 @@ typedef struct bh_stats {
   uint32_t steps;
   uint32_t retries;            /* node-arena growths performed by bh_step */
   uint32_t kernel_launches;    /* libbhgpu kernels launched by the call */
+  uint64_t walk_cell_evals;    /* cell entries the walk evaluated, 32 lane slots each */
+  uint64_t walk_point_evals;   /* point entries the walk evaluated, 32 lane slots each */
 } bh_stats;
 
 typedef struct bh_node {

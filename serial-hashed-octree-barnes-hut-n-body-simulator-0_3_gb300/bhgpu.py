@@ -64,7 +64,8 @@ class Stats(ctypes.Structure):
                 ("n_nodes", ctypes.c_uint64), ("n_leaves", ctypes.c_uint64),
                 ("interactions_cell", ctypes.c_uint64), ("interactions_p2p", ctypes.c_uint64),
                 ("max_depth", ctypes.c_uint32), ("error_flags", ctypes.c_uint32), ("steps", ctypes.c_uint32),
-                ("retries", ctypes.c_uint32), ("kernel_launches", ctypes.c_uint32)]
+                ("retries", ctypes.c_uint32), ("kernel_launches", ctypes.c_uint32),
+                ("walk_cell_evals", ctypes.c_uint64), ("walk_point_evals", ctypes.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

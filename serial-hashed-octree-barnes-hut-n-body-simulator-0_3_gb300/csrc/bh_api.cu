@@ -539,6 +539,8 @@ bh_status bh_force(bh_ctx* c, double theta, double eps, float* acc4_out, bh_stat
     st->ms_step = st->ms_walk;
     st->interactions_cell = c->h_counters->cell;
     st->interactions_p2p = c->h_counters->p2p;
+    st->walk_cell_evals = c->h_counters->cell_evals;
+    st->walk_point_evals = c->h_counters->point_evals;
     st->n_nodes = (uint64_t)c->h_level_bounds[kLevels];
     st->error_flags = e;
     st->kernel_launches = 1;
@@ -631,6 +633,8 @@ bh_status bh_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
       st->n_nodes = (uint64_t)c->h_level_bounds[kLevels];
       st->interactions_cell += c->h_counters->cell;
       st->interactions_p2p += c->h_counters->p2p;
+      st->walk_cell_evals += c->h_counters->cell_evals;
+      st->walk_point_evals += c->h_counters->point_evals;
       st->max_depth = std::max(st->max_depth, c->h_counters->max_depth);
       st->steps++;
     }

@@ -56,6 +56,8 @@ struct __align__(16) NodeF64 {
 struct Counters {
   unsigned long long cell;
   unsigned long long p2p;
+  unsigned long long cell_evals;   // warp-wide cell entries evaluated (32 lane slots each)
+  unsigned long long point_evals;  // warp-wide point entries evaluated
   unsigned int group_next;  // walk work queue
   unsigned int max_depth;
 };

@@ -6,19 +6,26 @@
 // existing child with the MAC size^2 / d^2 < theta^2 against the body; accepted children go
 // to the body's interaction list, the others are pushed; a popped leaf is added unless it is
 // the body itself (same position). Here the warp walks once for its 32 bodies and every stack
-// entry carries the 32-bit mask of lanes for which the node is still open. Each child is
-// tested by every lane of the mask (one broadcast load, one ballot): lanes that accept it
-// record it as a multipole interaction with that lane mask, the remaining lanes open it. So
-// every lane ends up with exactly the interaction set the reference builds for its body.
+// entry carries the 32-bit mask of lanes for which the node is still open, so each lane ends
+// up with exactly the interaction set the reference builds for its body.
 //
-// Interactions are buffered per warp in shared memory, 32 at a time: each lane stages one
-// node's data (a broadcast-free coalesced gather), then all lanes run over the buffer, and a
-// lane adds an entry's term only when its bit is set in that entry's mask. Two buffers:
+// Traversal, per round: the warp pops stack entries until their children fill the 32 lanes,
+// each lane loads one child and classifies it against the bounding box of the group's bodies:
+//   accept-all  the MAC holds even at the box's nearest point -> accepted by every open lane
+//   open-all    the MAC fails even at the box's farthest corner -> opened by every open lane
+//   mixed       otherwise: the child is broadcast and every lane runs its own MAC (a ballot)
+// (both bounds carry a 1e-5 relative margin, so they agree with the per-lane FP32 test). The
+// outcomes are appended to shared-memory buffers with warp-wide prefix counts:
 //   cells  : accepted nodes with more than one body — monopole + quadrupole (intended mode)
-//   points : single bodies — accepted single-body leaves, members of opened leaves, and (in
-//            literal mode) every accepted node as a point mass at its pseudo-barycentre.
-// Points at exactly the lane's own position contribute nothing (the reference's self-skip).
-// Sums are FP32 per buffer flush, added into Kahan-compensated per-lane totals.
+//   points : single bodies — accepted single-body leaves, the members of opened leaves, and
+//            (literal mode) every accepted node as a point mass at its pseudo-barycentre
+// and opened internal children are pushed with their child range, so a pop needs no load.
+//
+// Evaluation: a full buffer (32 entries) is staged through shared memory, one entry per lane,
+// and every lane runs over all 32 entries, adding an entry's term when its bit is set in the
+// entry's mask. Sums are FP32 per flush, added into Kahan-compensated per-lane totals. With a
+// positive softening a point at the lane's own position contributes exactly 0, so the
+// self-skip test is only compiled in for zero softening.
 #include <cuda_runtime.h>
 
 #include "bh_internal.cuh"
@@ -28,19 +35,25 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kStack = 192;  // >= 7 * 21 + 8: LIFO walk keeps at most 7 pending siblings per depth
-constexpr int kPtBuf = 64;
+constexpr int kStack = 384;
+constexpr int kStackDeep = 160;  // above this depth the warp pops one entry per round (DFS bound)
+constexpr int kBuf = 64;
+constexpr uint32_t kChildShift = 28;  // stack entry: first_child | nchild << 28
+constexpr float kMacMargin = 1e-5f;
 
 struct WarpSmem {
-  int stack_node[kStack];
-  unsigned stack_mask[kStack];
-  int cell_node[32];
-  unsigned cell_mask[32];
-  int pt_idx[kPtBuf];  // >= 0: body (tree order); < 0: -(node + 1)
-  unsigned pt_mask[kPtBuf];
+  uint32_t stk_node[kStack];
+  uint32_t stk_mask[kStack];
+  int cell_node[kBuf];
+  uint32_t cell_mask[kBuf];
+  int pt_idx[kBuf];  // >= 0: body (tree order); < 0: -(node + 1)
+  uint32_t pt_mask[kBuf];
   float4 st0[32];
   float4 st1[32];
   float4 st2[32];
+  int ex_first[32];
+  int ex_off[32];
+  uint32_t ex_mask[32];
 };
 
 struct Acc {
@@ -60,51 +73,57 @@ struct Acc {
   }
 };
 
-__device__ __forceinline__ void flush_cells(WarpSmem& s, int ncell, const WalkNode* __restrict__ nodes, int lane,
-                                            float px, float py, float pz, float eps2, Acc& acc, unsigned& cnt) {
+// 32 multipole cells (monopole + quadrupole). The lane mask rides in st2.w.
+__device__ __forceinline__ void eval_cells(WarpSmem& s, int cnt, const WalkNode* __restrict__ nodes,
+                                           uint32_t lanebit, float px, float py, float pz, float eps2, Acc& acc,
+                                           unsigned long long& ev) {
+  ev += (unsigned)cnt;
   __syncwarp();
-  if (lane < ncell) {
+  const int lane = __ffs(lanebit) - 1;
+  if (lane < cnt) {
     const WalkNode* nd = nodes + s.cell_node[lane];
     s.st0[lane] = __ldg(&nd->mac);
     s.st1[lane] = __ldg(&nd->mq);
-    s.st2[lane] = __ldg(&nd->q2);
+    float4 q2 = __ldg(&nd->q2);
+    q2.w = __uint_as_float(s.cell_mask[lane]);
+    s.st2[lane] = q2;
   }
   __syncwarp();
   float bx = 0.f, by = 0.f, bz = 0.f;
-  for (int j = 0; j < ncell; ++j) {
-    const unsigned mk = s.cell_mask[j];
+#pragma unroll 2
+  for (int j = 0; j < cnt; ++j) {
     const float4 c0 = s.st0[j], c1 = s.st1[j], c2 = s.st2[j];
     const float dx = c0.x - px, dy = c0.y - py, dz = c0.z - pz;
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
     const float rinv = rsqrtf(r2);
-    const float rinv2 = rinv * rinv;
-    const float rinv3 = rinv * rinv2;
-    const float rinv5 = rinv3 * rinv2;
+    const float u = rinv * rinv;   // 1 / D^2
+    const float w3 = rinv * u;     // 1 / D^3
+    const float w5 = w3 * u;       // 1 / D^5
     // Q.d with Q = (Qxx, Qxy, Qxz, Qyy, Qyz, Qzz) = (c1.y, c1.z, c1.w, c2.x, c2.y, c2.z)
     const float qx = fmaf(c1.y, dx, fmaf(c1.z, dy, c1.w * dz));
     const float qy = fmaf(c1.z, dx, fmaf(c2.x, dy, c2.y * dz));
     const float qz = fmaf(c1.w, dx, fmaf(c2.y, dy, c2.z * dz));
     const float qr = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
-    // a += m d / D^3 - Q.d / D^5 + 2.5 (d.Q.d) d / D^7
-    const float radial = fmaf(c1.x, rinv3, 2.5f * qr * rinv5 * rinv2);
-    const float fx = fmaf(radial, dx, -qx * rinv5);
-    const float fy = fmaf(radial, dy, -qy * rinv5);
-    const float fz = fmaf(radial, dz, -qz * rinv5);
-    if ((mk >> lane) & 1u) {
-      bx += fx;
-      by += fy;
-      bz += fz;
-      ++cnt;
+    // a += d (m / D^3 + 2.5 (d.Q.d) / D^7) - Q.d / D^5
+    const float radial = fmaf(qr, w5 * (2.5f * u), c1.x * w3);
+    if (__float_as_uint(c2.w) & lanebit) {
+      bx = fmaf(-w5, qx, fmaf(radial, dx, bx));
+      by = fmaf(-w5, qy, fmaf(radial, dy, by));
+      bz = fmaf(-w5, qz, fmaf(radial, dz, bz));
     }
   }
   acc.add(bx, by, bz);
 }
 
-__device__ __forceinline__ void flush_points(WarpSmem& s, int npt, const WalkNode* __restrict__ nodes,
-                                             const float4* __restrict__ tpos, int lane, float px, float py,
-                                             float pz, float eps2, Acc& acc, unsigned& cnt) {
+// Up to 32 point masses. The lane mask is read from pt_mask.
+template <bool kSelfTest>
+__device__ __forceinline__ void eval_points(WarpSmem& s, int cnt, const WalkNode* __restrict__ nodes,
+                                            const float4* __restrict__ tpos, uint32_t lanebit, float px, float py,
+                                            float pz, float eps2, Acc& acc, unsigned long long& ev) {
+  ev += (unsigned)cnt;
   __syncwarp();
-  if (lane < npt) {
+  const int lane = __ffs(lanebit) - 1;
+  if (lane < cnt) {
     const int e = s.pt_idx[lane];
     float4 v;
     if (e >= 0) {
@@ -118,25 +137,43 @@ __device__ __forceinline__ void flush_points(WarpSmem& s, int npt, const WalkNod
   }
   __syncwarp();
   float bx = 0.f, by = 0.f, bz = 0.f;
-  for (int j = 0; j < npt; ++j) {
-    const unsigned mk = s.pt_mask[j];
+#pragma unroll 4
+  for (int j = 0; j < cnt; ++j) {
     const float4 v = s.st0[j];
+    const uint32_t mk = s.pt_mask[j];
     const float dx = v.x - px, dy = v.y - py, dz = v.z - pz;
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
     const float rinv = rsqrtf(r2);
     const float mr3 = v.w * rinv * rinv * rinv;
-    const bool self = (dx == 0.f) & (dy == 0.f) & (dz == 0.f);
-    if (((mk >> lane) & 1u) && !self) {
+    bool take = (mk & lanebit) != 0u;
+    if (kSelfTest) take = take && !((dx == 0.f) & (dy == 0.f) & (dz == 0.f));
+    if (take) {
       bx = fmaf(mr3, dx, bx);
       by = fmaf(mr3, dy, by);
       bz = fmaf(mr3, dz, bz);
-      ++cnt;
     }
   }
   acc.add(bx, by, bz);
 }
 
-template <bool kQuad>
+// Moves buffer entries [32, n) to [0, n - 32) after the first 32 were evaluated.
+__device__ __forceinline__ void shift_down(int* idx, uint32_t* msk, int n, int lane) {
+  __syncwarp();
+  const int rest = n - 32;
+  int e = 0;
+  uint32_t m = 0;
+  if (lane < rest) {
+    e = idx[32 + lane];
+    m = msk[32 + lane];
+  }
+  __syncwarp();
+  if (lane < rest) {
+    idx[lane] = e;
+    msk[lane] = m;
+  }
+}
+
+template <bool kQuad, bool kSelfTest>
 __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ nodes,
                                                    const float4* __restrict__ tpos,
                                                    const uint32_t* __restrict__ tslot, int n, float theta2,
@@ -145,121 +182,255 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
                                                    Counters* __restrict__ ctr, uint32_t* __restrict__ err) {
   __shared__ WarpSmem smem[kWarps];
   const int lane = threadIdx.x & 31;
+  const uint32_t lanebit = 1u << lane;
+  const uint32_t lt_mask = lanebit - 1u;
   WarpSmem& s = smem[threadIdx.x >> 5];
   if (*((volatile uint32_t*)err) & (kErrNodes | kErrTimeout)) return;
   const int ngroups = (n + 31) >> 5;
   const int4 root_link = __ldg(&nodes[0].link);
-  unsigned long long tot_cell = 0, tot_pt = 0;
+  const float acc_scale = theta2 * (1.f - kMacMargin);
+  const float open_scale = theta2 * (1.f + kMacMargin);
+  unsigned long long tot_cell = 0, tot_pt = 0, ev_cell = 0, ev_pt = 0;  // ev_*: warp-uniform
+  bool overflow = false;
 
   for (;;) {
     int g = 0;
     if (lane == 0) g = (int)atomicAdd(&ctr->group_next, 1u);
     g = __shfl_sync(0xffffffffu, g, 0);
     if (g >= ngroups) break;
-    const int i = g * 32 + lane;
+    const int gbase = g * 32;
+    const int i = gbase + lane;
     const bool valid = i < n;
-    const float4 p = valid ? __ldg(tpos + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const unsigned active = __ballot_sync(0xffffffffu, valid);
+    const float4 p = __ldg(tpos + (valid ? i : gbase));
+    const uint32_t active = __ballot_sync(0xffffffffu, valid);
+    // bounding box of the group's bodies
+    float bminx = p.x, bminy = p.y, bminz = p.z, bmaxx = p.x, bmaxy = p.y, bmaxz = p.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      bminx = fminf(bminx, __shfl_xor_sync(0xffffffffu, bminx, o));
+      bminy = fminf(bminy, __shfl_xor_sync(0xffffffffu, bminy, o));
+      bminz = fminf(bminz, __shfl_xor_sync(0xffffffffu, bminz, o));
+      bmaxx = fmaxf(bmaxx, __shfl_xor_sync(0xffffffffu, bmaxx, o));
+      bmaxy = fmaxf(bmaxy, __shfl_xor_sync(0xffffffffu, bmaxy, o));
+      bmaxz = fmaxf(bmaxz, __shfl_xor_sync(0xffffffffu, bmaxz, o));
+    }
     Acc acc;
-    unsigned cnt_cell = 0, cnt_pt = 0;
     int sp = 0, ncell = 0, npt = 0;
-    bool overflow = false;
-
-    auto append_points = [&](int first, int count, unsigned mask) {
-      for (int off = 0; off < count; off += 32) {
-        const int k = min(32, count - off);
-        __syncwarp();
-        if (lane < k) {
-          s.pt_idx[npt + lane] = first + off + lane;
-          s.pt_mask[npt + lane] = mask;
-        }
-        npt += k;
-        if (npt >= 32) {
-          flush_points(s, 32, nodes, tpos, lane, p.x, p.y, p.z, eps2, acc, cnt_pt);
-          __syncwarp();
-          const int rest = npt - 32;
-          if (lane < rest) {
-            const int e = s.pt_idx[32 + lane];
-            const unsigned m = s.pt_mask[32 + lane];
-            __syncwarp(__activemask());
-            s.pt_idx[lane] = e;
-            s.pt_mask[lane] = m;
-          }
-          npt = rest;
-        }
-      }
-    };
+    // per-lane shares of the group's interaction counts (each lane counts the entries it
+    // appended, times the lanes in their masks); self pairs are subtracted
+    long long cnt_cell = 0, cnt_pt = 0;
 
     if (root_link.y == 0) {
-      append_points(root_link.z, root_link.w, active);
+      // the root is a leaf: every lane sums all its bodies
+      for (int base = 0; base < root_link.w; base += 32) {
+        const int k = min(32, root_link.w - base);
+        __syncwarp();
+        if (lane < k) {
+          s.pt_idx[lane] = root_link.z + base + lane;
+          s.pt_mask[lane] = active;
+        }
+        if (lane == 0) cnt_pt += (long long)k * __popc(active);
+        eval_points<kSelfTest>(s, k, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt);
+      }
+      if (lane == 0) cnt_pt -= __popc(active);
     } else {
+      __syncwarp();
       if (lane == 0) {
-        s.stack_node[0] = 0;
-        s.stack_mask[0] = active;
+        s.stk_node[0] = (uint32_t)root_link.x | ((uint32_t)root_link.y << kChildShift);
+        s.stk_mask[0] = active;
       }
       sp = 1;
     }
+
     while (sp > 0) {
-      --sp;
       __syncwarp();
-      const int nd = s.stack_node[sp];
-      const unsigned m = s.stack_mask[sp];
-      const int4 link = __ldg(&nodes[nd].link);
-      for (int c = link.x; c < link.x + link.y; ++c) {
-        const float4 mac = __ldg(&nodes[c].mac);
-        const float dx = mac.x - p.x, dy = mac.y - p.y, dz = mac.z - p.z;
-        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const bool accept = fabsf(mac.w) < theta2 * d2;
-        const unsigned am = __ballot_sync(0xffffffffu, accept) & m;
-        const unsigned om = m & ~am;
-        if (am) {
-          if (!kQuad || mac.w < 0.f) {
-            __syncwarp();
-            if (lane == 0) {
-              s.pt_idx[npt] = -(c + 1);
-              s.pt_mask[npt] = am;
-            }
-            ++npt;
-            if (npt >= 32) {
-              flush_points(s, 32, nodes, tpos, lane, p.x, p.y, p.z, eps2, acc, cnt_pt);
-              npt = 0;
-            }
-          } else {
-            __syncwarp();
-            if (lane == 0) {
-              s.cell_node[ncell] = c;
-              s.cell_mask[ncell] = am;
-            }
-            ++ncell;
-            if (ncell == 32) {
-              flush_cells(s, 32, nodes, lane, p.x, p.y, p.z, eps2, acc, cnt_cell);
-              ncell = 0;
-            }
-          }
+      // ---- pop entries whose children fill at most 32 lanes
+      const int avail = min(sp, sp > kStackDeep ? 1 : 32);
+      uint32_t ent = 0, emask = 0;
+      int nch = 0;
+      if (lane < avail) {
+        ent = s.stk_node[sp - 1 - lane];
+        emask = s.stk_mask[sp - 1 - lane];
+        nch = (int)(ent >> kChildShift);
+      }
+      int incl = nch;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const uint32_t take = __ballot_sync(0xffffffffu, lane < avail && incl <= 32);
+      const int k = __popc(take);  // >= 1: one entry has at most 8 children
+      const int total = __shfl_sync(0xffffffffu, incl, k - 1);
+      sp -= k;
+      const int start = incl - nch;  // exclusive prefix
+      const uint32_t starts = __reduce_or_sync(0xffffffffu, (take & lanebit) ? (1u << start) : 0u);
+      // lane j < total handles child j: its entry is the number of starts at or below j, minus 1
+      const int my_e = __popc(starts & (lanebit | lt_mask)) - 1;
+      const int e_src = lane < total ? my_e : 0;
+      const uint32_t pent = __shfl_sync(0xffffffffu, ent, e_src);
+      const uint32_t pmask = __shfl_sync(0xffffffffu, emask, e_src);
+      const int pstart = __shfl_sync(0xffffffffu, start, e_src);
+      const bool has = lane < total;
+      const int c = has ? (int)(pent & ((1u << kChildShift) - 1u)) + (lane - pstart) : 0;
+
+      // ---- classify the child against the group's bounding box
+      float4 mac = make_float4(0.f, 0.f, 0.f, 0.f);
+      int4 link = make_int4(0, 0, 0, 0);
+      uint32_t am = 0, om = 0;
+      bool mixed = false;
+      if (has) {
+        mac = __ldg(&nodes[c].mac);
+        link = __ldg(&nodes[c].link);
+        const float s2 = fabsf(mac.w);
+        const float lx = fmaxf(fmaxf(bminx - mac.x, mac.x - bmaxx), 0.f);
+        const float ly = fmaxf(fmaxf(bminy - mac.y, mac.y - bmaxy), 0.f);
+        const float lz = fmaxf(fmaxf(bminz - mac.z, mac.z - bmaxz), 0.f);
+        const float hx = fmaxf(fabsf(mac.x - bminx), fabsf(mac.x - bmaxx));
+        const float hy = fmaxf(fabsf(mac.y - bminy), fabsf(mac.y - bmaxy));
+        const float hz = fmaxf(fabsf(mac.z - bminz), fabsf(mac.z - bmaxz));
+        const float dmin2 = fmaf(lx, lx, fmaf(ly, ly, lz * lz));
+        const float dmax2 = fmaf(hx, hx, fmaf(hy, hy, hz * hz));
+        if (s2 < acc_scale * dmin2) {
+          am = pmask;
+        } else if (s2 >= open_scale * dmax2) {
+          om = pmask;
+        } else {
+          mixed = true;
         }
-        if (om) {
-          const int4 cl = __ldg(&nodes[c].link);
-          if (cl.y > 0) {
-            if (sp >= kStack) {
-              overflow = true;
-              break;
-            }
-            __syncwarp();
-            if (lane == 0) {
-              s.stack_node[sp] = c;
-              s.stack_mask[sp] = om;
-            }
-            ++sp;
-          } else {
-            append_points(cl.z, cl.w, om);
+      }
+      // per-lane MAC for the mixed children, one ballot each
+      uint32_t mixed_bits = __ballot_sync(0xffffffffu, mixed);
+      while (mixed_bits) {
+        const int j = __ffs(mixed_bits) - 1;
+        mixed_bits &= mixed_bits - 1;
+        const float cx = __shfl_sync(0xffffffffu, mac.x, j);
+        const float cy = __shfl_sync(0xffffffffu, mac.y, j);
+        const float cz = __shfl_sync(0xffffffffu, mac.z, j);
+        const float s2 = fabsf(__shfl_sync(0xffffffffu, mac.w, j));
+        const uint32_t m = __shfl_sync(0xffffffffu, pmask, j);
+        const float dx = cx - p.x, dy = cy - p.y, dz = cz - p.z;
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const uint32_t a = __ballot_sync(0xffffffffu, s2 < theta2 * d2) & m;
+        if (lane == j) {
+          am = a;
+          om = m & ~a;
+        }
+      }
+
+      // ---- appends
+      const bool single = mac.w < 0.f;  // single-body leaf
+      const bool is_cell = kQuad && am != 0u && !single;
+      const bool is_npt = am != 0u && !is_cell;
+      const bool is_push = om != 0u && link.y > 0;
+      const bool is_leaf = om != 0u && link.y == 0;
+
+      if (kQuad) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, is_cell);
+        if (bal) {
+          __syncwarp();
+          if (is_cell) {
+            const int pos = ncell + __popc(bal & lt_mask);
+            s.cell_node[pos] = c;
+            s.cell_mask[pos] = am;
+            cnt_cell += __popc(am);
+          }
+          ncell += __popc(bal);
+          if (ncell >= 32) {
+            eval_cells(s, 32, nodes, lanebit, p.x, p.y, p.z, eps2, acc, ev_cell);
+            shift_down(s.cell_node, s.cell_mask, ncell, lane);
+            ncell -= 32;
           }
         }
       }
-      if (overflow) break;
+      {
+        const uint32_t bal = __ballot_sync(0xffffffffu, is_npt);
+        if (bal) {
+          __syncwarp();
+          if (is_npt) {
+            const int pos = npt + __popc(bal & lt_mask);
+            s.pt_idx[pos] = -(c + 1);
+            s.pt_mask[pos] = am;
+            cnt_pt += __popc(am);
+          }
+          npt += __popc(bal);
+          if (npt >= 32) {
+            eval_points<kSelfTest>(s, 32, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt);
+            shift_down(s.pt_idx, s.pt_mask, npt, lane);
+            npt -= 32;
+          }
+        }
+      }
+      {
+        const uint32_t bal = __ballot_sync(0xffffffffu, is_push);
+        if (bal) {
+          const int np = __popc(bal);
+          if (sp + np > kStack) {
+            overflow = true;
+            break;
+          }
+          __syncwarp();
+          if (is_push) {
+            const int pos = sp + __popc(bal & lt_mask);
+            s.stk_node[pos] = (uint32_t)link.x | ((uint32_t)link.y << kChildShift);
+            s.stk_mask[pos] = om;
+          }
+          sp += np;
+        }
+      }
+      {
+        // opened leaves: expand their bodies into the point buffer, 32 at a time
+        const int cntb = is_leaf ? link.w : 0;
+        int incb = cntb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          int y = __shfl_up_sync(0xffffffffu, incb, o);
+          if (lane >= o) incb += y;
+        }
+        const int totb = __shfl_sync(0xffffffffu, incb, 31);
+        if (totb > 0) {
+          if (is_leaf) {
+            // self pairs inside this leaf: lanes of the mask whose own body is a member
+            const int lo = max(link.z, gbase), hi = min(link.z + link.w, gbase + 32);
+            uint32_t own = 0;
+            if (hi > lo) own = (hi - lo >= 32 ? 0xffffffffu : ((1u << (hi - lo)) - 1u)) << (lo - gbase);
+            cnt_pt += (long long)cntb * __popc(om) - __popc(own & om);
+          }
+          __syncwarp();
+          s.ex_first[lane] = link.z;
+          s.ex_off[lane] = incb - cntb;
+          s.ex_mask[lane] = is_leaf ? om : 0u;
+          __syncwarp();
+          for (int base = 0; base < totb; base += 32) {
+            const int gi = base + lane;
+            const int kk = min(32, totb - base);
+            if (gi < totb) {
+              // owner: last lane whose exclusive offset is <= gi (empty lanes share offsets
+              // with their successor, so the search lands on the lane that owns gi)
+              int lo2 = 0, hi2 = 31;
+              while (lo2 < hi2) {
+                const int mid = (lo2 + hi2 + 1) >> 1;
+                if (s.ex_off[mid] <= gi)
+                  lo2 = mid;
+                else
+                  hi2 = mid - 1;
+              }
+              s.pt_idx[npt + lane] = s.ex_first[lo2] + (gi - s.ex_off[lo2]);
+              s.pt_mask[npt + lane] = s.ex_mask[lo2];
+            }
+            npt += kk;
+            if (npt >= 32) {
+              eval_points<kSelfTest>(s, 32, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt);
+              shift_down(s.pt_idx, s.pt_mask, npt, lane);
+              npt -= 32;
+            }
+            __syncwarp();
+          }
+        }
+      }
     }
-    if (ncell > 0) flush_cells(s, ncell, nodes, lane, p.x, p.y, p.z, eps2, acc, cnt_cell);
-    if (npt > 0) flush_points(s, npt, nodes, tpos, lane, p.x, p.y, p.z, eps2, acc, cnt_pt);
-    if (overflow && lane == 0) atomicOr(err, kErrStack);
+    if (ncell > 0) eval_cells(s, ncell, nodes, lanebit, p.x, p.y, p.z, eps2, acc, ev_cell);
+    if (npt > 0) eval_points<kSelfTest>(s, npt, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt);
     if (valid) {
       const uint32_t slot = __ldg(tslot + i);
       const float ax = acc.sx, ay = acc.sy, az = acc.sz;
@@ -271,35 +442,47 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
         v.z += az * half_dt;
         vel_kick[slot] = v;
       }
-      tot_cell += cnt_cell;
-      tot_pt += cnt_pt;
     }
+    tot_cell += (unsigned long long)cnt_cell;
+    tot_pt += (unsigned long long)cnt_pt;
+    if (overflow) break;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    tot_cell += __shfl_down_sync(0xffffffffu, tot_cell, o);
-    tot_pt += __shfl_down_sync(0xffffffffu, tot_pt, o);
+    tot_cell += __shfl_xor_sync(0xffffffffu, tot_cell, o);
+    tot_pt += __shfl_xor_sync(0xffffffffu, tot_pt, o);
   }
-  if (lane == 0 && (tot_cell | tot_pt)) {
-    atomicAdd(&ctr->cell, tot_cell);
-    atomicAdd(&ctr->p2p, tot_pt);
+  if (lane == 0) {
+    if (overflow) atomicOr(err, kErrStack);
+    if (tot_cell | tot_pt) {
+      atomicAdd(&ctr->cell, tot_cell);
+      atomicAdd(&ctr->p2p, tot_pt);
+    }
+    if (ev_cell | ev_pt) {
+      atomicAdd(&ctr->cell_evals, ev_cell);
+      atomicAdd(&ctr->point_evals, ev_pt);
+    }
   }
 }
 
-int walk_grid(bool quad) {
-  static int blocks[2] = {0, 0};
-  int& b = blocks[quad ? 1 : 0];
-  if (b == 0) {
+template <bool kQuad, bool kSelf>
+int walk_grid() {
+  static int blocks = 0;
+  if (blocks == 0) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (quad)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<true>, kThreads, 0);
-    else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<false>, kThreads, 0);
-    b = max(1, sms * max(1, per_sm));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<kQuad, kSelf>, kThreads, 0);
+    blocks = max(1, sms * max(1, per_sm));
   }
-  return b;
+  return blocks;
+}
+
+template <bool kQuad, bool kSelf>
+void launch_walk_t(bh_ctx* c, int n, float theta2, float eps2, float4* acc_slot, float4* vel_kick, float half_dt) {
+  const int grid = min(walk_grid<kQuad, kSelf>(), (n + 31) / 32 / kWarps + 1);
+  k_walk<kQuad, kSelf><<<grid, kThreads, 0, c->stream>>>(c->wnode, c->tpos, c->tslot, n, theta2, eps2, acc_slot,
+                                                         vel_kick, half_dt, c->counters, c->err);
 }
 
 }  // namespace
@@ -308,16 +491,21 @@ void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc
                  float half_dt) {
   if (n <= 0) return;
   cudaMemsetAsync(&c->counters->group_next, 0, sizeof(unsigned), c->stream);
+  c->launches += 1;
   const float theta2 = theta * theta, eps2 = eps * eps;
   const bool quad = mode == BH_MULTIPOLE_QUADRUPOLE;
-  const int grid = min(walk_grid(quad), (n + 31) / 32 / kWarps + 1);
-  c->launches += 1;
-  if (quad)
-    k_walk<true><<<grid, kThreads, 0, c->stream>>>(c->wnode, c->tpos, c->tslot, n, theta2, eps2, acc_slot,
-                                                   vel_kick, half_dt, c->counters, c->err);
-  else
-    k_walk<false><<<grid, kThreads, 0, c->stream>>>(c->wnode, c->tpos, c->tslot, n, theta2, eps2, acc_slot,
-                                                    vel_kick, half_dt, c->counters, c->err);
+  const bool self = !(eps2 > 0.f);
+  if (quad) {
+    if (self)
+      launch_walk_t<true, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt);
+    else
+      launch_walk_t<true, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt);
+  } else {
+    if (self)
+      launch_walk_t<false, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt);
+    else
+      launch_walk_t<false, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt);
+  }
 }
 
 }  // namespace bh
