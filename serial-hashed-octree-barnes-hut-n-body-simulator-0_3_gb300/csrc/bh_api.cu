@@ -66,7 +66,7 @@ bh_status ensure_nodes(bh_ctx* c, size_t need) {
   dfree(c->nkey);
   dfree(c->nrange);
   dfree(c->wnode);
-  dfree(c->nf64);
+  dfree(c->nup);
   dfree(c->nchildbyte);
   dfree(c->hash_keys);
   dfree(c->hash_vals);
@@ -76,7 +76,7 @@ bh_status ensure_nodes(bh_ctx* c, size_t need) {
   BH_TRY(dalloc(&c->nkey, cap));
   BH_TRY(dalloc(&c->nrange, cap));
   BH_TRY(dalloc(&c->wnode, cap));
-  BH_TRY(dalloc(&c->nf64, cap));
+  BH_TRY(dalloc(&c->nup, cap));
   BH_TRY(dalloc(&c->nchildbyte, cap));
   c->node_cap = cap;
   c->tree_valid = false;
@@ -190,7 +190,7 @@ bh_status bh_destroy(bh_ctx* c) {
   dfree(c->nkey);
   dfree(c->nrange);
   dfree(c->wnode);
-  dfree(c->nf64);
+  dfree(c->nup);
   dfree(c->nchildbyte);
   dfree(c->lb_level);
   dfree(c->level_bounds);
@@ -447,17 +447,17 @@ bh_status bh_tree_nodes(bh_ctx* c, size_t cap, uint64_t* keys, int64_t* counts, 
   if (m == 0) return BH_OK;
   cudaSetDevice(c->device);
   std::vector<int2> r(m);
-  std::vector<bh::NodeF64> f(m);
+  std::vector<bh::NodeUp> f(m);
   if (keys) cudaMemcpyAsync(keys, c->nkey, sizeof(uint64_t) * m, cudaMemcpyDeviceToHost, c->stream);
   if (child_byte) cudaMemcpyAsync(child_byte, c->nchildbyte, m, cudaMemcpyDeviceToHost, c->stream);
   cudaMemcpyAsync(r.data(), c->nrange, sizeof(int2) * m, cudaMemcpyDeviceToHost, c->stream);
-  cudaMemcpyAsync(f.data(), c->nf64, sizeof(bh::NodeF64) * m, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(f.data(), c->nup, sizeof(bh::NodeUp) * m, cudaMemcpyDeviceToHost, c->stream);
   BH_TRY(cuda_status(cudaStreamSynchronize(c->stream)));
   for (size_t j = 0; j < m; ++j) {
     if (counts) counts[j] = r[j].y;
-    if (mass) mass[j] = f[j].mass;
+    if (mass) mass[j] = (double)f[j].mass_hi + (double)f[j].mass_lo;
     if (com3)
-      for (int a = 0; a < 3; ++a) com3[3 * j + a] = f[j].com[a];
+      for (int a = 0; a < 3; ++a) com3[3 * j + a] = (double)f[j].com_hi[a] + (double)f[j].com_lo[a];
     if (quad6)
       for (int k = 0; k < 6; ++k) quad6[6 * j + k] = f[j].q[k];
   }
@@ -487,17 +487,17 @@ bh_status bh_node_lookup(bh_ctx* c, uint64_t key, bh_node* out) {
   BH_TRY(last_launch());
   if (idx < 0) return BH_ERR_NOT_FOUND;
   int2 r;
-  bh::NodeF64 f;
+  bh::NodeUp f;
   uint8_t cb = 0;
   cudaMemcpy(&r, c->nrange + idx, sizeof(r), cudaMemcpyDeviceToHost);
-  cudaMemcpy(&f, c->nf64 + idx, sizeof(f), cudaMemcpyDeviceToHost);
+  cudaMemcpy(&f, c->nup + idx, sizeof(f), cudaMemcpyDeviceToHost);
   cudaMemcpy(&cb, c->nchildbyte + idx, 1, cudaMemcpyDeviceToHost);
   BH_TRY(last_launch());
   std::memset(out, 0, sizeof(*out));
   out->key = key;
   out->count = r.y;
-  out->mass = f.mass;
-  for (int a = 0; a < 3; ++a) out->com[a] = f.com[a];
+  out->mass = (double)f.mass_hi + (double)f.mass_lo;
+  for (int a = 0; a < 3; ++a) out->com[a] = (double)f.com_hi[a] + (double)f.com_lo[a];
   for (int k = 0; k < 6; ++k) out->quad[k] = f.q[k];
   out->child_byte = cb;
   // node bounds from the key, by the reference's child-centre recurrence

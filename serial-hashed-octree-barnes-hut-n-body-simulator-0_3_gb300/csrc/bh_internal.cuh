@@ -44,11 +44,16 @@ struct __align__(16) WalkNode {
   int4 link;
 };
 
-// FP64 multipole of one node, kept for the parents during the upsweep.
-struct __align__(16) NodeF64 {
-  double com[3];
-  double mass;
-  double q[6];
+// Multipole of one node, kept for the parents during the upsweep (64 bytes). Mass and
+// centre of mass are float-float pairs (value = hi + lo, about 44 significant bits, from
+// compensated FP32 sums: GB300's FP64 pipe is far too slow for this pass); the quadrupole is
+// FP32. hi is the FP32 rounding of the pair, which is what the walk reads.
+struct __align__(16) NodeUp {
+  float com_hi[3];
+  float mass_hi;
+  float com_lo[3];
+  float mass_lo;
+  float q[6];         // Qxx, Qxy, Qxz, Qyy, Qyz, Qzz about the centre of mass
   uint32_t min_rank;  // smallest Morton slot among members (literal barycentre)
   uint32_t pad;
 };
@@ -105,7 +110,7 @@ struct bh_ctx {
   uint64_t* nkey = nullptr;
   int2* nrange = nullptr;  // first body, body count
   bh::WalkNode* wnode = nullptr;
-  bh::NodeF64* nf64 = nullptr;
+  bh::NodeUp* nup = nullptr;
   uint8_t* nchildbyte = nullptr;
   uint32_t* lb_level = nullptr;  // look-back words of the level build
   int lb_level_tiles = 0;

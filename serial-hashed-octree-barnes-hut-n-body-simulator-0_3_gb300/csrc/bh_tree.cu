@@ -151,19 +151,27 @@ __global__ __launch_bounds__(kThreads) void k_bounds_partial(const float4* __res
   }
 }
 
-// Combines the partials in block order: centre = sum * (1 / N) (Vec3D::operator/=,
-// src/MathUtils.cpp:81-90), size = max(0, max_a (max_i |p_ia| - c_a)). fl(|p| - c) is
-// monotone in |p|, so the maximum over bodies of the rounded differences equals the rounded
-// difference of the maximum.
+// Combines the partials (one warp: lane l sums partials l, l + 32, ... in order, then a fixed
+// shuffle tree; deterministic, and only ~15 dependent FP64 additions deep): centre = sum *
+// (1 / N) (Vec3D::operator/=, src/MathUtils.cpp:81-90), size = max(0, max_a (max_i |p_ia| -
+// c_a)). fl(|p| - c) is monotone in |p|, so the maximum over bodies of the rounded differences
+// equals the rounded difference of the maximum.
 __global__ void k_bounds_final(const double* __restrict__ partial, int blocks, int n, double edge_factor,
                                Geom* __restrict__ g) {
-  if (threadIdx.x != 0) return;
+  const int lane = threadIdx.x;
   double s[3] = {0, 0, 0}, m[3] = {0, 0, 0};
-  for (int b = 0; b < blocks; ++b)
+  for (int b = lane; b < blocks; b += 32)
     for (int a = 0; a < 3; ++a) {
       s[a] = __dadd_rn(s[a], partial[b * 6 + a]);
       m[a] = fmax(m[a], partial[b * 6 + 3 + a]);
     }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    for (int a = 0; a < 3; ++a) {
+      s[a] = __dadd_rn(s[a], __shfl_down_sync(0xffffffffu, s[a], o));
+      m[a] = fmax(m[a], __shfl_down_sync(0xffffffffu, m[a], o));
+    }
+  if (lane != 0) return;
   double c[3] = {s[0], s[1], s[2]};
   double nn = (double)n;
   if (nn != 0) {
@@ -445,24 +453,62 @@ __global__ __launch_bounds__(kThreads) void k_level(int d, const uint64_t* __res
 // upsweep
 // ---------------------------------------------------------------------------------------
 
-// Parallel-axis quadrupole contribution of one child (or member body) of mass m at offset x
-// from the node's centre of mass, the reference's formulas (src/HashedOctree.cpp:778-808).
-__device__ __forceinline__ void quad_add(double q[6], double m, double x, double y, double z) {
-  q[1] += 3.0 * m * (x * y);
-  q[2] += 3.0 * m * (x * z);
-  q[4] += 3.0 * m * (y * z);
-  double xx = x * x, yy = y * y, zz = z * z;
-  double d2 = (xx + yy + zz) * m;
-  double m3 = m * 3.0;
-  q[0] += m3 * xx - d2;
-  q[3] += m3 * yy - d2;
-  q[5] += m3 * zz - d2;
+// Float-float arithmetic (a value is hi + lo): TwoSum (Knuth), FMA-based TwoProduct and a
+// Newton-corrected quotient (Dekker 1971). About 44 significant bits from FP32 operations.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_norm(float s, float e) {
+  const float hi = s + e;
+  return {hi, e - (hi - s)};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e += a.lo + b.lo;
+  return ff_norm(s, e);
+}
+__device__ __forceinline__ FF ff_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return ff_norm(p, e);
+}
+__device__ __forceinline__ FF ff_div(FF n, FF d) {
+  const float q = n.hi / d.hi;
+  const float p = q * d.hi;
+  const float pe = fmaf(q, d.hi, -p);
+  const float r = (((n.hi - p) - pe) + fmaf(-q, d.lo, n.lo)) / d.hi;
+  return ff_norm(q, r);
 }
 
+// Parallel-axis quadrupole contribution of one child (or member body) of mass m at offset x
+// from the node's centre of mass, the reference's formulas (src/HashedOctree.cpp:778-808).
+__device__ __forceinline__ void quad_add(float q[6], float m, float x, float y, float z) {
+  const float m3 = 3.f * m;
+  q[1] = fmaf(m3 * x, y, q[1]);
+  q[2] = fmaf(m3 * x, z, q[2]);
+  q[4] = fmaf(m3 * y, z, q[4]);
+  const float r2m = m * fmaf(x, x, fmaf(y, y, z * z));
+  q[0] += fmaf(m3 * x, x, -r2m);
+  q[3] += fmaf(m3 * y, y, -r2m);
+  q[5] += fmaf(m3 * z, z, -r2m);
+}
+
+// One depth of the bottom-up multipole pass (computeTreeBaryCenters / computeNodeBaryCenters,
+// src/HashedOctree.cpp:721-855, as intended; or the literal pseudo-barycentres). Leaves
+// combine their member bodies, internal nodes their children (depth d + 1, done by the
+// previous launch).
 __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int* __restrict__ level_bounds,
                                                       const float4* __restrict__ tpos,
                                                       const uint32_t* __restrict__ tslot,
-                                                      WalkNode* __restrict__ wn, NodeF64* __restrict__ nf,
+                                                      WalkNode* __restrict__ wn, NodeUp* __restrict__ nf,
                                                       const Geom* __restrict__ g, const uint32_t* __restrict__ err,
                                                       Counters* __restrict__ ctr) {
   if (*err & kErrNodes) return;
@@ -473,100 +519,95 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&ctr->max_depth, (unsigned)d);
   for (int node = lo + blockIdx.x * kThreads + threadIdx.x; node < hi; node += gridDim.x * kThreads) {
     const int4 link = wn[node].link;
-    double com[3] = {0, 0, 0}, mass = 0, q[6] = {0, 0, 0, 0, 0, 0};
+    FF mass = {0.f, 0.f}, com[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    float q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     uint32_t min_rank = 0xffffffffu;
     bool single = false;
     if (link.y == 0) {  // leaf: members are tree-order bodies [link.z, link.z + link.w)
       if (mode == BH_MULTIPOLE_LITERAL) {
         int first = link.z;
         for (int b = link.z; b < link.z + link.w; ++b) {
-          mass += (double)tpos[b].w;
-          uint32_t rk = tslot[b];
+          mass = ff_add(mass, {tpos[b].w, 0.f});
+          const uint32_t rk = tslot[b];
           if (rk < min_rank) {
             min_rank = rk;
             first = b;
           }
         }
-        float4 p = tpos[first];
-        com[0] = p.x;
-        com[1] = p.y;
-        com[2] = p.z;
+        const float4 p = tpos[first];
+        com[0] = {p.x, 0.f};
+        com[1] = {p.y, 0.f};
+        com[2] = {p.z, 0.f};
         single = link.w == 1;
       } else if (link.w == 1) {
-        float4 p = tpos[link.z];
-        com[0] = p.x;
-        com[1] = p.y;
-        com[2] = p.z;
-        mass = p.w;
+        const float4 p = tpos[link.z];
+        com[0] = {p.x, 0.f};
+        com[1] = {p.y, 0.f};
+        com[2] = {p.z, 0.f};
+        mass = {p.w, 0.f};
         min_rank = tslot[link.z];
         single = true;
       } else {
         for (int b = link.z; b < link.z + link.w; ++b) {
-          float4 p = tpos[b];
-          mass += (double)p.w;
-          com[0] += (double)p.x * (double)p.w;
-          com[1] += (double)p.y * (double)p.w;
-          com[2] += (double)p.z * (double)p.w;
+          const float4 p = tpos[b];
+          mass = ff_add(mass, {p.w, 0.f});
+          com[0] = ff_add(com[0], ff_prod(p.x, p.w));
+          com[1] = ff_add(com[1], ff_prod(p.y, p.w));
+          com[2] = ff_add(com[2], ff_prod(p.z, p.w));
           min_rank = min(min_rank, tslot[b]);
         }
-        if (mass != 0) {
-          double inv = 1.0 / mass;
-          com[0] *= inv;
-          com[1] *= inv;
-          com[2] *= inv;
-        }
+        if (mass.hi != 0.f)
+          for (int a = 0; a < 3; ++a) com[a] = ff_div(com[a], mass);
         for (int b = link.z; b < link.z + link.w; ++b) {
-          float4 p = tpos[b];
-          quad_add(q, (double)p.w, (double)p.x - com[0], (double)p.y - com[1], (double)p.z - com[2]);
+          const float4 p = tpos[b];
+          quad_add(q, p.w, (p.x - com[0].hi) - com[0].lo, (p.y - com[1].hi) - com[1].lo,
+                   (p.z - com[2].hi) - com[2].lo);
         }
       }
     } else {
       if (mode == BH_MULTIPOLE_LITERAL) {
         for (int c = link.x; c < link.x + link.y; ++c) {
-          const NodeF64& ch = nf[c];
-          mass += ch.mass;
+          const NodeUp& ch = nf[c];
+          mass = ff_add(mass, {ch.mass_hi, ch.mass_lo});
           if (ch.min_rank < min_rank) {
             min_rank = ch.min_rank;
-            com[0] = ch.com[0];
-            com[1] = ch.com[1];
-            com[2] = ch.com[2];
+            for (int a = 0; a < 3; ++a) com[a] = {ch.com_hi[a], ch.com_lo[a]};
           }
         }
       } else {
         for (int c = link.x; c < link.x + link.y; ++c) {
-          const NodeF64& ch = nf[c];
-          mass += ch.mass;
-          com[0] += ch.com[0] * ch.mass;
-          com[1] += ch.com[1] * ch.mass;
-          com[2] += ch.com[2] * ch.mass;
+          const NodeUp& ch = nf[c];
+          const FF m = {ch.mass_hi, ch.mass_lo};
+          mass = ff_add(mass, m);
+          for (int a = 0; a < 3; ++a) com[a] = ff_add(com[a], ff_mul({ch.com_hi[a], ch.com_lo[a]}, m));
           min_rank = min(min_rank, ch.min_rank);
         }
-        if (mass != 0) {
-          double inv = 1.0 / mass;
-          com[0] *= inv;
-          com[1] *= inv;
-          com[2] *= inv;
-        }
+        if (mass.hi != 0.f)
+          for (int a = 0; a < 3; ++a) com[a] = ff_div(com[a], mass);
         for (int c = link.x; c < link.x + link.y; ++c) {
-          const NodeF64& ch = nf[c];
-          quad_add(q, ch.mass, ch.com[0] - com[0], ch.com[1] - com[1], ch.com[2] - com[2]);
+          const NodeUp& ch = nf[c];
+          quad_add(q, ch.mass_hi, (ch.com_hi[0] - com[0].hi) + (ch.com_lo[0] - com[0].lo),
+                   (ch.com_hi[1] - com[1].hi) + (ch.com_lo[1] - com[1].lo),
+                   (ch.com_hi[2] - com[2].hi) + (ch.com_lo[2] - com[2].lo));
           if (wn[c].link.w > 1)
             for (int k = 0; k < 6; ++k) q[k] += ch.q[k];
         }
       }
     }
-    NodeF64 out;
-    out.com[0] = com[0];
-    out.com[1] = com[1];
-    out.com[2] = com[2];
-    out.mass = mass;
+    NodeUp out;
+    for (int a = 0; a < 3; ++a) {
+      out.com_hi[a] = com[a].hi;
+      out.com_lo[a] = com[a].lo;
+    }
+    out.mass_hi = mass.hi;
+    out.mass_lo = mass.lo;
     for (int k = 0; k < 6; ++k) out.q[k] = q[k];
     out.min_rank = min_rank;
     out.pad = 0;
     nf[node] = out;
-    wn[node].mac = make_float4((float)com[0], (float)com[1], (float)com[2], single ? -s2 : s2);
-    wn[node].mq = make_float4((float)mass, (float)q[0], (float)q[1], (float)q[2]);
-    wn[node].q2 = make_float4((float)q[3], (float)q[4], (float)q[5], 0.f);
+    wn[node].mac = make_float4(com[0].hi, com[1].hi, com[2].hi, single ? -s2 : s2);
+    wn[node].mq = make_float4(mass.hi, q[0], q[1], q[2]);
+    wn[node].q2 = make_float4(q[3], q[4], q[5], 0.f);
   }
 }
 
@@ -720,7 +761,7 @@ void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode) {
   const int grid = 152 * 8;
   c->launches += kLevels;
   for (int d = kMaxDepth; d >= 0; --d)
-    k_upsweep<<<grid, kThreads, 0, c->stream>>>(d, mode, c->level_bounds, c->tpos, c->tslot, c->wnode, c->nf64,
+    k_upsweep<<<grid, kThreads, 0, c->stream>>>(d, mode, c->level_bounds, c->tpos, c->tslot, c->wnode, c->nup,
                                                 c->geom, c->err, c->counters);
 }
 
