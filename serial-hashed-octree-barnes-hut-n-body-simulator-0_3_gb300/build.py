@@ -24,10 +24,16 @@ def _nvcc():
     return cand
 
 
+# Per-file flags. The walk flushes FP32 denormals to zero: every quantity it handles (positions,
+# masses, softened distances, multipoles) is many orders of magnitude above the denormal range,
+# and without denormal support rsqrtf and the FP32 arithmetic need fewer instructions.
+FILE_FLAGS = {"bh_walk.cu": ["-ftz=true"]}
+
+
 def _compile(src, extra):
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
     cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
-           "-I" + os.path.join(ROOT, "include"), "-c", os.path.join(CSRC, src), "-o", obj] + extra
+           "-I" + os.path.join(ROOT, "include"), "-c", os.path.join(CSRC, src), "-o", obj] + FILE_FLAGS.get(src, []) + extra
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

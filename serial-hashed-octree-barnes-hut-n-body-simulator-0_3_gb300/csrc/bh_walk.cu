@@ -90,7 +90,7 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cnt, const WalkNode*
   }
   __syncwarp();
   float bx = 0.f, by = 0.f, bz = 0.f;
-#pragma unroll 2
+#pragma unroll 8
   for (int j = 0; j < cnt; ++j) {
     const float4 c0 = s.st0[j], c1 = s.st1[j], c2 = s.st2[j];
     const float dx = c0.x - px, dy = c0.y - py, dz = c0.z - pz;
@@ -106,11 +106,14 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cnt, const WalkNode*
     const float qr = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
     // a += d (m / D^3 + 2.5 (d.Q.d) / D^7) - Q.d / D^5
     const float radial = fmaf(qr, w5 * (2.5f * u), c1.x * w3);
-    if (__float_as_uint(c2.w) & lanebit) {
-      bx = fmaf(-w5, qx, fmaf(radial, dx, bx));
-      by = fmaf(-w5, qy, fmaf(radial, dy, by));
-      bz = fmaf(-w5, qz, fmaf(radial, dz, bz));
-    }
+    // selects rather than a branch: every lane runs the same straight-line code
+    const bool take = (__float_as_uint(c2.w) & lanebit) != 0u;
+    const float tx = fmaf(-w5, qx, fmaf(radial, dx, bx));
+    const float ty = fmaf(-w5, qy, fmaf(radial, dy, by));
+    const float tz = fmaf(-w5, qz, fmaf(radial, dz, bz));
+    bx = take ? tx : bx;
+    by = take ? ty : by;
+    bz = take ? tz : bz;
   }
   acc.add(bx, by, bz);
 }
