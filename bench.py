@@ -43,6 +43,11 @@ WORKLOADS = {
                        desc="Plummer sphere N=2^22, theta=0.5, eps=0.005, leaf 16, dt=5e-4, quadrupole, edge 2S"),
     "plummer-16k": dict(n=16384, theta=0.5, eps=0.01, leaf=1, dt=1e-3, edge=2.0, kind="plummer", seed=0,
                         desc="Plummer sphere N=16384, theta=0.5, eps=0.01, leaf 1, dt=1e-3, quadrupole, edge 2S"),
+    # profiling sizes of the headline recipe (small enough for full ncu captures / larger than L2)
+    "plummer-1m": dict(n=1 << 20, theta=0.5, eps=0.005, leaf=16, dt=5e-4, edge=2.0, kind="plummer", seed=0,
+                       desc="Plummer sphere N=2^20, theta=0.5, eps=0.005, leaf 16, dt=5e-4, quadrupole, edge 2S"),
+    "plummer-8m": dict(n=1 << 23, theta=0.5, eps=0.005, leaf=16, dt=5e-4, edge=2.0, kind="plummer", seed=0,
+                       desc="Plummer sphere N=2^23, theta=0.5, eps=0.005, leaf 16, dt=5e-4, quadrupole, edge 2S"),
     "two-spheres-4m": dict(n=1 << 22, theta=0.5, eps=0.001, leaf=8, dt=2e-4, edge=2.0, kind="two", seed=0,
                            desc="two Plummer spheres of 2^21 (B: a=0.1, M=0.1 at (10,0,0)), theta=0.5, "
                                 "eps=0.001, leaf 8, dt=2e-4"),
@@ -168,12 +173,16 @@ def measured_peaks():
 
 
 def ncu_traffic():
-    """DRAM bytes per walk launch from the committed ncu summary, scaled per body."""
+    """DRAM bytes per body of one walk launch, from the committed ncu summary (a line
+    'walk_dram_bytes_per_body: X'), or None."""
     try:
-        with open(os.path.join(ROOT, "profiles", "walk_traffic.json")) as f:
-            return json.load(f)
+        with open(os.path.join(ROOT, "profiles", "k_walk_quadrupole_plummer1m.md")) as f:
+            for line in f:
+                if line.startswith("walk_dram_bytes_per_body:"):
+                    return {"bytes_per_body": float(line.split(":")[1])}
     except Exception:
-        return None
+        pass
+    return None
 
 
 def accuracy_vs_direct(w, pm, acc, orc, nthreads, ntarget=1024):
