@@ -202,6 +202,24 @@ bh_status bh_host_free(void* ptr);
  * kernel timed with CUDA events on the context's stream. */
 bh_status bh_measure_fp32_peak(bh_ctx* ctx, double* tflops);
 
+/* Allocation-free stable sort of (key, value) pairs in caller-owned device memory. It has no
+ * counterpart in the reference. It is meant for callers that cannot call cudaMalloc where
+ * they need the sort: per-frame loops and stream-callback chains, where an allocation or free
+ * would synchronise the whole device, and embedders with a fixed device-memory budget. The
+ * sort's scratch (ping-pong buffers, histograms, look-back words) lives in a fixed device
+ * array of the library, which each GPU holds while the library is loaded, so n is limited to
+ * BH_SORT_STATIC_MAX_KEYS (larger n returns BH_ERR_INVALID_ARG). Sorts stably by the full
+ * 64-bit key (the same permutation as bh_sort_bodies) into keys_out / vals_out; the inputs
+ * are left unchanged; asynchronous on `stream` (a cudaStream_t, NULL for the legacy default
+ * stream) on the current device. status_out (optional, device memory) becomes nonzero if a
+ * device-side wait gave up, in which case the output is unspecified.
+ * The first call on each device looks up the scratch array's device address, so make it before
+ * any stream capture on that device. Every call reuses the same scratch: calls that can overlap
+ * on the GPU (unordered streams, concurrent host threads) race, and the caller must order them. */
+#define BH_SORT_STATIC_MAX_KEYS 65536
+bh_status bh_sort_keys_static(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
+                              uint32_t* vals_out, size_t n, void* stream, uint32_t* status_out);
+
 /* Host-side synthetic initial conditions (set-up time, not the per-step path): a Plummer
  * sphere of n bodies, scale radius a, total mass mtot, shifted to its centre-of-mass frame,
  * then offset by pos_offset3 / vel_offset3 (either may be null). */

@@ -37,7 +37,7 @@ EXPORTS = [
     "bh_sort_bodies", "bh_build", "bh_tree_size", "bh_tree_nodes", "bh_node_lookup", "bh_force",
     "bh_kick_drift", "bh_kick", "bh_step", "bh_params_default", "bh_synchronize", "bh_event_record",
     "bh_event_elapsed_ms", "bh_flush_l2", "bh_host_alloc", "bh_host_free", "bh_measure_fp32_peak",
-    "bh_plummer",
+    "bh_plummer", "bh_sort_keys_static",
 ]
 
 
@@ -119,6 +119,7 @@ def load():
         "bh_host_free": ([P], I),
         "bh_measure_fp32_peak": ([P, ctypes.POINTER(D)], I),
         "bh_plummer": ([ctypes.c_uint64, S, D, D, P, P, P, P], I),
+        "bh_sort_keys_static": ([P, P, P, P, S, P, P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

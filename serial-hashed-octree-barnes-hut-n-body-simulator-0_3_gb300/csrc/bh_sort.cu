@@ -11,6 +11,8 @@
 // then item, then lane, which is the load order), and tiles are ordered by the look-back.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "bh_internal.cuh"
 
 namespace bh {
@@ -268,3 +270,114 @@ void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t*
 }
 
 }  // namespace bh
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free sort entry point (bh_sort_keys_static, include/bhgpu.h).
+//
+// Some callers cannot call cudaMalloc at the point where they need a sort: code running in
+// a per-frame loop or a chain of stream callbacks, where cudaMalloc / cudaFree would
+// synchronise the whole device and stall other streams, and embedders that reserve a fixed
+// device-memory budget up front and forbid allocations afterwards. For them this variant keeps
+// every scratch buffer the sort needs (ping-pong key/value buffers, digit histograms, look-back
+// words, tile counters, error word) in one file-scope __device__ array of fixed size, which
+// the GPU holds for as long as the library is loaded. The caller passes only its inputs and
+// outputs.
+//
+// The array's name in host code is only a host-side stand-in for the symbol, not a device
+// address; the device address is resolved with cudaGetSymbolAddress the first time the entry
+// point runs on a device (with that device current) and cached per device. That first call
+// therefore has to happen outside any stream capture. All calls share the one array and each
+// call overwrites it, so calls that could overlap on the GPU (different streams without
+// ordering, or different host threads) race and must be serialised by the caller.
+// ---------------------------------------------------------------------------------------
+namespace bh {
+namespace {
+
+constexpr size_t kStaticMaxKeys = BH_SORT_STATIC_MAX_KEYS;
+constexpr int kStaticTiles = (int)((kStaticMaxKeys + kTile - 1) / kTile);
+constexpr size_t kOffTmpKeys = 0;
+constexpr size_t kOffTmpVals = kOffTmpKeys + kStaticMaxKeys * sizeof(uint64_t);
+constexpr size_t kOffHist = kOffTmpVals + kStaticMaxKeys * sizeof(uint32_t);
+constexpr size_t kOffLookback = kOffHist + (size_t)kPasses * kRadix * sizeof(uint32_t);
+constexpr size_t kOffTileCtr = kOffLookback + (size_t)kPasses * kStaticTiles * kRadix * sizeof(uint32_t);
+constexpr size_t kOffErr = kOffTileCtr + kPasses * sizeof(uint32_t);
+constexpr size_t kStaticBytes = kOffErr + 256;
+
+static __device__ __align__(256) unsigned char g_static_sort_scratch[kStaticBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+unsigned char* g_static_addr[kMaxDevices] = {};
+bool g_static_attr[kMaxDevices] = {};
+
+}  // namespace
+}  // namespace bh
+
+extern "C" bh_status bh_sort_keys_static(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
+                                         uint32_t* vals_out, size_t n, void* stream, uint32_t* status_out) {
+  using namespace bh;
+  if (n > kStaticMaxKeys) return BH_ERR_INVALID_ARG;
+  if (n > 0 && (!keys_in || !vals_in || !keys_out || !vals_out)) return BH_ERR_INVALID_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return BH_ERR_DEVICE;
+  }
+  unsigned char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_addr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_static_sort_scratch) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return BH_ERR_DEVICE;
+      }
+      g_static_addr[dev] = (unsigned char*)p;
+    }
+    if (!g_static_attr[dev]) {
+      if (cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)sizeof(OnesweepSmem)) != cudaSuccess) {
+        cudaGetLastError();
+        return BH_ERR_DEVICE;
+      }
+      g_static_attr[dev] = true;
+    }
+    base = g_static_addr[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nn = (int)n;
+  if (nn <= 1 && status_out) cudaMemsetAsync(status_out, 0, sizeof(uint32_t), st);
+  if (nn == 0) return cudaGetLastError() == cudaSuccess ? BH_OK : BH_ERR_DEVICE;
+  if (nn == 1) {
+    cudaMemcpyAsync(keys_out, keys_in, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(vals_out, vals_in, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+    return cudaGetLastError() == cudaSuccess ? BH_OK : BH_ERR_DEVICE;
+  }
+  uint64_t* tmp_keys = (uint64_t*)(base + kOffTmpKeys);
+  uint32_t* tmp_vals = (uint32_t*)(base + kOffTmpVals);
+  uint32_t* hist = (uint32_t*)(base + kOffHist);
+  uint32_t* lookback = (uint32_t*)(base + kOffLookback);
+  uint32_t* tile_ctr = (uint32_t*)(base + kOffTileCtr);
+  uint32_t* err = status_out ? status_out : (uint32_t*)(base + kOffErr);
+  const int tiles = sort_max_tiles(n);
+  // everything that must start at zero: histograms, look-back words, tile counters, error word
+  cudaMemsetAsync(hist, 0, kOffErr + sizeof(uint32_t) - kOffHist, st);
+  if (status_out) cudaMemsetAsync(status_out, 0, sizeof(uint32_t), st);
+  const int hblocks = (int)min((long long)152 * 4, ((long long)nn + kThreads * 8 - 1) / (kThreads * 8));
+  k_hist<<<hblocks, kThreads, 0, st>>>(keys_in, nn, hist);
+  k_hist_scan<<<kPasses, kRadix, 0, st>>>(hist);
+  // pass p reads from (p == 0 ? input : buffer of pass p - 1) and writes the tmp buffers on
+  // even passes and the caller's output on odd ones; 8 passes end in the output
+  const uint64_t* ka = keys_in;
+  const uint32_t* va = vals_in;
+  for (int p = 0; p < kPasses; ++p) {
+    uint64_t* kb = (p & 1) ? keys_out : tmp_keys;
+    uint32_t* vb = (p & 1) ? vals_out : tmp_vals;
+    k_onesweep<<<tiles, kThreads, sizeof(OnesweepSmem), st>>>(ka, va, kb, vb, nn, 8 * p, hist + p * kRadix,
+                                                              lookback + (size_t)p * tiles * kRadix,
+                                                              tile_ctr + p, err);
+    ka = kb;
+    va = vb;
+  }
+  return cudaGetLastError() == cudaSuccess ? BH_OK : BH_ERR_DEVICE;
+}
