@@ -390,21 +390,129 @@ def run_ours(args, w, dist):
     sim.close()
 
 
+ENSEMBLE = dict(nsys=4096, nmin=256, nmax=65536, theta=0.6, eps=0.01, leaf=8, dt=1e-3, edge=2.0, seed=1000,
+                desc="4096 Plummer systems (seed 1000 + s), N_s = round(exp(U ln 256 + ln 256)) in [256, 65536], "
+                     "M = a = 1 each, theta=0.6, eps=0.01, leaf 8, dt=1e-3, quadrupole, edge 2S")
+
+
+def make_ensemble(bh, e):
+    import concurrent.futures
+
+    rng = np.random.default_rng(e["seed"])
+    u = rng.uniform(0.0, 1.0, e["nsys"])
+    sizes = np.round(np.exp(u * np.log(e["nmax"] / e["nmin"]) + np.log(e["nmin"]))).astype(np.int64)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint32)
+    pos = np.zeros((int(off[-1]), 4), np.float32)
+    vel = np.zeros_like(pos)
+
+    def one(s):
+        p, v = bh.plummer(e["seed"] + s, int(sizes[s]))
+        pos[off[s]:off[s + 1]] = p
+        vel[off[s]:off[s + 1]] = v
+
+    with concurrent.futures.ThreadPoolExecutor(os.cpu_count() or 4) as ex:
+        list(ex.map(one, range(e["nsys"])))
+    return pos, vel, off
+
+
+def run_ensemble(args, dist):
+    """Batched ensemble: all systems in one bh_batch_step per step (graph-replayed), against the
+    plain path looped over the systems (each system resident in its own context, one bh_step
+    call per system per step, wall-clock), estimated from a seeded sample of systems."""
+    import __graft_entry__
+
+    bh = __graft_entry__.package()
+    bh.load()
+    e = ENSEMBLE
+    pos, vel, off = make_ensemble(bh, e)
+    n = int(off[-1])
+    prm = bh.default_params(theta=e["theta"], eps=e["eps"], dt=e["dt"], leaf_capacity=e["leaf"],
+                            multipole=bh.BH_MULTIPOLE_QUADRUPOLE, edge_factor=e["edge"], acc_follows_body=1)
+    sim = bh.Simulation(n)
+    sim.batch_set(pos, vel, off)
+    fp32_peak = sim.fp32_peak_tflops()
+    for _ in range(args.warmup):
+        sim.batch_step(prm, 1, stats=False)
+    per_step, flops = [], []
+    dist.barrier()
+    with ClockSampler(int(os.environ.get("BH_GPU_INDEX", "0"))) as clocks:
+        for _ in range(args.steps):
+            sim.flush_l2()
+            st = sim.batch_step(prm, 1)
+            per_step.append(st.ms_step)
+            flops.append(FLOPS_P2P * st.interactions_p2p + FLOPS_CELL_QUAD * st.interactions_cell)
+    total_ms = dist.max(sum(per_step))
+    value = dist.sum(n * args.steps) / (total_ms * 1e-3)
+    # end to end: upload (pinned) + one batched step + download
+    pp, pv = bh.PinnedArray((n, 4)), bh.PinnedArray((n, 4))
+    pp.array[:] = pos
+    pv.array[:] = vel
+    e2e = []
+    for _ in range(3):
+        sim.event_record(0)
+        sim.batch_set(pp.array, pv.array, off)
+        sim.batch_step(prm, 1, stats=False)
+        sim.get_bodies()
+        sim.event_record(1)
+        e2e.append(sim.event_elapsed_ms(0, 1))
+    pp.free()
+    pv.free()
+    sim.close()
+    # the plain path looped over the systems, on a seeded sample of systems
+    rng = np.random.default_rng(7)
+    sample = np.sort(rng.choice(e["nsys"], args.loop_sample, replace=False))
+    loop_s = []
+    for s in sample:
+        a, b = int(off[s]), int(off[s + 1])
+        with bh.Simulation(b - a) as one:
+            one.set_bodies(pos[a:b], vel[a:b])
+            for _ in range(2):
+                one.step(prm, 1, stats=False)
+            t = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                one.step(prm, 1, stats=False)
+                t.append(time.perf_counter() - t0)
+            loop_s.append(statistics.median(t))
+    loop_step_s = sum(loop_s) * e["nsys"] / len(sample)
+    walk_tflops = statistics.mean(flops) / (statistics.mean(per_step) * 1e-3) / 1e12
+    if dist.rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "ours",
+                "config": {"workload": "ensemble-4096", "systems": e["nsys"], "bodies": n, "desc": e["desc"],
+                           "timing": "per-step CUDA events around the graph launch; L2 flushed between steps"},
+                "e2e": {"value": n / (statistics.median(e2e) * 1e-3), "unit": "body-steps/s",
+                        "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 48 * n,
+                        "ms_per_step": statistics.median(e2e)},
+                "plain_loop": {"value": n / loop_step_s, "unit": "body-steps/s", "seconds_per_step": loop_step_s,
+                               "sample": f"{len(sample)} seeded systems, each in its own context, wall-clock bh_step "
+                                         f"(median of 3), sum scaled by {e['nsys']}/{len(sample)}"},
+                "batched_speedup_vs_plain_loop": loop_step_s / (total_ms / args.steps * 1e-3),
+                "flops_per_step": statistics.mean(flops), "tflops": walk_tflops,
+                "fp32_peak_tflops": fp32_peak, "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="plummer-4m", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="plummer-4m", choices=sorted(WORKLOADS) + ["ensemble-4096"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--cpu-walk-sample", type=int, default=16384)
+    ap.add_argument("--loop-sample", type=int, default=128)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warning: fewer than 3 warm-up steps")
-    w = WORKLOADS[args.workload]
     dist = Dist()
+    if args.workload == "ensemble-4096":
+        run_ensemble(args, dist)
+        return
+    w = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, w, dist)
     else:

@@ -183,6 +183,17 @@ bh_status bh_kick(bh_ctx* ctx, double dt);
  * force -> kick. stats (optional) is filled for the call. */
 bh_status bh_step(bh_ctx* ctx, const bh_params* params, int nsteps, bh_stats* stats);
 
+/* Batched ensembles (no counterpart in the reference, which simulates one system): nsys
+ * independent systems in one context, system s owning bodies [sys_offsets[s],
+ * sys_offsets[s+1]) (host array of nsys + 1 entries, sys_offsets[0] = 0, every system non-empty,
+ * nsys <= 65535). bh_batch_set uploads them (like bh_set_bodies); bh_batch_step advances all
+ * systems nsteps frames with bh_step's per-system semantics, in one set of launches per step
+ * (captured once in a CUDA graph and replayed). Bodies never leave their system's range; within
+ * it they end in the system's Morton order. bh_get_bodies downloads the whole ensemble. */
+bh_status bh_batch_set(bh_ctx* ctx, const float* pos_m4, const float* vel4, const uint32_t* sys_offsets,
+                       size_t nsys);
+bh_status bh_batch_step(bh_ctx* ctx, const bh_params* params, int nsteps, bh_stats* stats);
+
 /* Default parameters: theta 0.5, eps 0.025, dt 1e-3, leaf 1, quadrupole, edge 2, acc follows body. */
 void bh_params_default(bh_params* p);
 

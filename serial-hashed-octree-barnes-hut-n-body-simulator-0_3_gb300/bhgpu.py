@@ -37,7 +37,7 @@ EXPORTS = [
     "bh_sort_bodies", "bh_build", "bh_tree_size", "bh_tree_nodes", "bh_node_lookup", "bh_force",
     "bh_kick_drift", "bh_kick", "bh_step", "bh_params_default", "bh_synchronize", "bh_event_record",
     "bh_event_elapsed_ms", "bh_flush_l2", "bh_host_alloc", "bh_host_free", "bh_measure_fp32_peak",
-    "bh_plummer", "bh_sort_keys_static",
+    "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step",
 ]
 
 
@@ -120,6 +120,8 @@ def load():
         "bh_measure_fp32_peak": ([P, ctypes.POINTER(D)], I),
         "bh_plummer": ([ctypes.c_uint64, S, D, D, P, P, P, P], I),
         "bh_sort_keys_static": ([P, P, P, P, S, P, P], I),
+        "bh_batch_set": ([P, P, P, P, S], I),
+        "bh_batch_step": ([P, ctypes.POINTER(Params), I, ctypes.POINTER(Stats)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -275,6 +277,19 @@ class Simulation:
         st = Stats()
         check(self.lib.bh_step(self.h, ctypes.byref(params), nsteps, ctypes.byref(st) if stats else None),
               "bh_step")
+        return st
+
+    def batch_set(self, pos_m, vel, offsets):
+        """Uploads an ensemble: system s owns rows offsets[s]:offsets[s + 1]."""
+        pos_m = np.ascontiguousarray(pos_m, np.float32)
+        vel = np.ascontiguousarray(vel, np.float32)
+        off = np.ascontiguousarray(offsets, np.uint32)
+        check(self.lib.bh_batch_set(self.h, _ptr(pos_m), _ptr(vel), _ptr(off), len(off) - 1), "bh_batch_set")
+
+    def batch_step(self, params, nsteps=1, stats=True):
+        st = Stats()
+        check(self.lib.bh_batch_step(self.h, ctypes.byref(params), nsteps, ctypes.byref(st) if stats else None),
+              "bh_batch_step")
         return st
 
     def synchronize(self):

@@ -62,6 +62,11 @@ __global__ void k_iota(uint32_t* v, int n) {
 
 bh_status ensure_nodes(bh_ctx* c, size_t need) {
   if (c->node_cap >= need && c->nkey) return BH_OK;
+  for (auto& g : c->graph)  // captured graphs hold the old node pointers
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
   size_t cap = std::max<size_t>(need, 1024);
   dfree(c->nkey);
   dfree(c->nrange);
@@ -197,6 +202,12 @@ bh_status bh_destroy(bh_ctx* c) {
   dfree(c->level_tile_ctr);
   dfree(c->hash_keys);
   dfree(c->hash_vals);
+  for (auto& g : c->graph)
+    if (g) cudaGraphExecDestroy(g);
+  dfree(c->sys_off);
+  dfree(c->sys_geom);
+  dfree(c->body_sys);
+  dfree(c->groups);
   dfree(c->geom);
   dfree(c->bounds_partial);
   dfree(c->err);
@@ -219,6 +230,8 @@ bh_status bh_create(bh_ctx** out, size_t capacity, int device) {
     return BH_ERR_DEVICE;
   }
   if (cudaSetDevice(device) != cudaSuccess) return BH_ERR_DEVICE;
+  bh::sort_init();
+  bh::walk_init();
   bh_ctx* c = new (std::nothrow) bh_ctx();
   if (!c) return BH_ERR_OOM;
   c->device = device;
@@ -283,6 +296,12 @@ bh_status bh_set_state(bh_ctx* c, const float* pos_m4, const float* vel4, const 
   c->n = n;
   c->cur = 0;
   c->tree_valid = false;
+  c->batch = false;
+  for (auto& g : c->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
   if (n > 0) {
     cudaMemcpyAsync(c->pos[0], pos_m4, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(c->vel[0], vel4, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream);
@@ -715,6 +734,163 @@ bh_status bh_measure_fp32_peak(bh_ctx* c, double* tflops) {
   const double flops = (double)blocks * 256 * 4096 * 16 * 8 * 2;
   *tflops = flops / (ms * 1e-3) / 1e12;
   return BH_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Batched ensembles: many independent systems in one context, stepped together. Each system
+// keeps a fixed body range [off[s], off[s+1]); every stage runs over all bodies at once:
+// per-system bounds; Morton keys with the system's own cube; a stable sort by key followed by
+// a stable sort by system id, which regroups every system in key order inside its range; the
+// same for tree keys; one tree level build for all systems together (one root per system);
+// one walk over groups of up to 32 bodies that never straddle a system, pulled from a global
+// work queue. Each step is captured once per state parity in a CUDA graph and replayed.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kMaxSystems = 65535;  // system ids are stored as u16
+
+void destroy_graphs(bh_ctx* c) {
+  for (auto& g : c->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+bool same_params(const bh_params& a, const bh_params& b) {
+  return a.theta == b.theta && a.eps == b.eps && a.dt == b.dt && a.leaf_capacity == b.leaf_capacity &&
+         a.multipole == b.multipole && a.edge_factor == b.edge_factor && a.acc_follows_body == b.acc_follows_body;
+}
+
+// One batched step, enqueued on c->stream without host synchronisation (capturable).
+void enqueue_batch_step(bh_ctx* c, const bh_params& p) {
+  const int n = (int)c->n, nx = 1 - c->cur;
+  const float dt = (float)p.dt;
+  clear_device_flags(c);
+  bh::launch_batch_bounds(c, c->pos[c->cur], p.edge_factor);
+  bh::launch_morton(c, c->pos[c->cur], n, c->keys[0], c->vals[0], true);
+  uint64_t* ko;
+  uint32_t* vo;
+  bh::radix_sort_pairs(c, c->keys[0], c->vals[0], c->keys[1], c->vals[1], n, c->stream, &ko, &vo);
+  bh::launch_sys_keys(c, c->vals[0], n, c->keys[1]);
+  bh::radix_sort_pairs(c, c->keys[1], c->vals[0], c->keys[0], c->vals[1], n, c->stream, &ko, &vo, 0, 2);
+  // vals[0]: (system, Morton key) order; keys[0] receives the per-slot tree keys
+  bh::launch_gather_kd_treekey(c, c->vals[0], n, c->pos[c->cur], c->vel[c->cur], c->acc, p.acc_follows_body, dt,
+                               c->pos[nx], c->vel[nx], c->keys[0], c->tslot, true);
+  cudaMemcpyAsync(c->tkey, c->keys[0], sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, c->stream);
+  bh::radix_sort_pairs(c, c->tkey, c->tslot, c->keys[1], c->vals[1], n, c->stream, &ko, &vo);
+  bh::launch_sys_keys(c, c->tslot, n, c->keys[1]);
+  bh::radix_sort_pairs(c, c->keys[1], c->tslot, c->tkey, c->vals[1], n, c->stream, &ko, &vo, 0, 2);
+  bh::launch_gather_tree_keys(c, c->tslot, n, c->pos[nx], c->keys[0], c->tpos, c->tkey);
+  bh::launch_build(c, n, p.leaf_capacity, true);
+  bh::launch_upsweep(c, n, p.leaf_capacity, p.multipole, true);
+  bh::launch_walk(c, n, (float)p.theta, (float)p.eps, p.multipole, c->acc, c->vel[nx], 0.5f * dt, true);
+}
+
+}  // namespace
+
+extern "C" {
+
+bh_status bh_batch_set(bh_ctx* c, const float* pos_m4, const float* vel4, const uint32_t* sys_offsets,
+                       size_t nsys) {
+  if (!c || !sys_offsets || nsys == 0 || nsys > kMaxSystems || sys_offsets[0] != 0) return BH_ERR_INVALID_ARG;
+  for (size_t s = 0; s < nsys; ++s)
+    if (sys_offsets[s + 1] <= sys_offsets[s]) return BH_ERR_INVALID_ARG;  // every system has a body
+  const size_t n = sys_offsets[nsys];
+  if (n > c->cap) return BH_ERR_INVALID_ARG;
+  BH_TRY(bh_set_state(c, pos_m4, vel4, nullptr, n));
+  cudaSetDevice(c->device);
+  destroy_graphs(c);
+  if (c->sys_cap < nsys) {
+    dfree(c->sys_off);
+    dfree(c->sys_geom);
+    c->sys_cap = 0;
+    BH_TRY(dalloc(&c->sys_off, nsys + 1));
+    BH_TRY(dalloc(&c->sys_geom, nsys));
+    c->sys_cap = nsys;
+  }
+  if (!c->body_sys) BH_TRY(dalloc(&c->body_sys, c->cap));
+  std::vector<uint16_t> bs(n);
+  std::vector<int4> groups;
+  for (size_t s = 0; s < nsys; ++s) {
+    const uint32_t b0 = sys_offsets[s], b1 = sys_offsets[s + 1];
+    for (uint32_t i = b0; i < b1; ++i) bs[i] = (uint16_t)s;
+    for (uint32_t g = b0; g < b1; g += 32) groups.push_back(make_int4((int)g, (int)std::min(32u, b1 - g), (int)s, (int)s));
+  }
+  dfree(c->groups);
+  BH_TRY(dalloc(&c->groups, groups.size()));
+  c->ngroups = (int)groups.size();
+  cudaMemcpyAsync(c->sys_off, sys_offsets, sizeof(uint32_t) * (nsys + 1), cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->body_sys, bs.data(), sizeof(uint16_t) * n, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->groups, groups.data(), sizeof(int4) * groups.size(), cudaMemcpyHostToDevice, c->stream);
+  BH_TRY(cuda_status(cudaStreamSynchronize(c->stream)));
+  c->nsys = (int)nsys;
+  c->batch = true;
+  return BH_OK;
+}
+
+bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
+  if (!c || !prm || nsteps < 0 || !c->batch || prm->leaf_capacity < 1 || !(prm->theta >= 0) || !(prm->eps >= 0) ||
+      !(prm->edge_factor > 0) ||
+      (prm->multipole != BH_MULTIPOLE_LITERAL && prm->multipole != BH_MULTIPOLE_QUADRUPOLE))
+    return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (c->n == 0 || nsteps == 0) return BH_OK;
+  const size_t need = std::max<size_t>(2 * c->n + 64 * (size_t)c->nsys, 1024);
+  if (c->node_cap < need) destroy_graphs(c);
+  BH_TRY(ensure_nodes(c, need));
+  if (!same_params(c->graph_params, *prm)) destroy_graphs(c);
+  c->graph_params = *prm;
+  const uint64_t launches0 = c->launches;
+  for (int s = 0; s < nsteps; ++s) {
+    uint32_t e = 0;
+    for (;;) {
+      const int par = c->cur;
+      if (!c->graph[par]) {
+        cudaGraph_t g = nullptr;
+        BH_TRY(cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)));
+        enqueue_batch_step(c, *prm);
+        cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+        if (ce != cudaSuccess || !g) return cuda_status(ce == cudaSuccess ? cudaErrorUnknown : ce);
+        ce = cudaGraphInstantiate(&c->graph[par], g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+          c->graph[par] = nullptr;
+          return cuda_status(ce);
+        }
+      }
+      if (st) cudaEventRecord(c->stage_ev[0], c->stream);
+      BH_TRY(cuda_status(cudaGraphLaunch(c->graph[par], c->stream)));
+      if (st) cudaEventRecord(c->stage_ev[1], c->stream);
+      BH_TRY(sync_and_check(c, &e));
+      if (e & bh::kErrNodes) {  // arena too small: grow it, re-capture, redo the step
+        destroy_graphs(c);
+        BH_TRY(ensure_nodes(c, c->node_cap * 2));
+        if (st) st->retries++;
+        continue;
+      }
+      break;
+    }
+    if (e) return err_to_status(e);
+    c->cur = 1 - c->cur;
+    if (st) {
+      st->ms_step += elapsed(c, 0, 1);
+      st->n_nodes = (uint64_t)c->h_level_bounds[kLevels];
+      st->interactions_cell += c->h_counters->cell;
+      st->interactions_p2p += c->h_counters->p2p;
+      st->walk_cell_evals += c->h_counters->cell_evals;
+      st->walk_point_evals += c->h_counters->point_evals;
+      st->max_depth = std::max(st->max_depth, c->h_counters->max_depth);
+      st->steps++;
+    }
+  }
+  if (st) st->kernel_launches = (uint32_t)(c->launches - launches0);
+  c->tree_valid = false;  // the ensemble's tree is not a single-system tree
+  c->hash_valid = false;
+  return last_launch();
 }
 
 }  // extern "C"

@@ -139,32 +139,53 @@ struct bh_ctx {
 
   void* flush_buf = nullptr;
   size_t flush_bytes = 0;
+
+  // batched ensemble (bh_batch_*): system s owns the fixed body range [sys_off[s], sys_off[s+1])
+  bool batch = false;
+  int nsys = 0;
+  uint32_t* sys_off = nullptr;     // device [nsys + 1]
+  uint16_t* body_sys = nullptr;    // device, system of each body slot / tree position
+  bh::Geom* sys_geom = nullptr;    // device [nsys]
+  int4* groups = nullptr;          // device walk groups: first body, body count, root node, system
+  int ngroups = 0;
+  size_t sys_cap = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // captured batched step, by state parity
+  bh_params graph_params = {};
   uint64_t launches = 0;  // kernels launched on this context (every launcher adds its count)
 };
 
 namespace bh {
 
 // Kernel launchers (defined in the .cu files; all asynchronous on `st`).
+// Stable LSD radix sort by 8-bit digits first_pass .. first_pass + npasses - 1 of the keys
+// (all 8 digits by default). With an even pass count the result is back in keys_in / vals_in.
 void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t* keys_tmp, uint32_t* vals_tmp,
-                      int n, cudaStream_t st, uint64_t** keys_out, uint32_t** vals_out);
+                      int n, cudaStream_t st, uint64_t** keys_out, uint32_t** vals_out, int first_pass = 0,
+                      int npasses = 8);
 int sort_max_tiles(size_t n);
+void sort_init();
+void walk_init();
 
 void launch_bounds(bh_ctx* c, const float4* pos, int n, double edge_factor);
 void launch_set_geom(bh_ctx* c, const double center[3], double size, const double tcenter[3], double tedge);
-void launch_morton(bh_ctx* c, const float4* pos, int n, uint64_t* keys, uint32_t* idx);
+void launch_morton(bh_ctx* c, const float4* pos, int n, uint64_t* keys, uint32_t* idx, bool batch = false);
 void launch_gather(bh_ctx* c, const uint32_t* perm, int n, const float4* pin, const float4* vin, float4* pout,
                    float4* vout);
 void launch_gather_kd_treekey(bh_ctx* c, const uint32_t* perm, int n, const float4* pin, const float4* vin,
                               const float4* acc, int acc_follows_body, float dt, float4* pout, float4* vout,
-                              uint64_t* tkeys, uint32_t* tidx);
+                              uint64_t* tkeys, uint32_t* tidx, bool batch = false);
 void launch_treekey(bh_ctx* c, const float4* pos, int n, uint64_t* tkeys, uint32_t* tidx);
 void launch_kick_drift(bh_ctx* c, float4* pos, float4* vel, const float4* acc, int n, float dt, int drift);
 void launch_gather_tree(bh_ctx* c, const uint32_t* tslot, int n, const float4* pos, float4* tpos);
-void launch_build(bh_ctx* c, int n, int leaf_cap);
-void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode);
+void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch = false);
+void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode, bool batch = false);
+void launch_batch_bounds(bh_ctx* c, const float4* pos, double edge_factor);
+void launch_sys_keys(bh_ctx* c, const uint32_t* vals, int n, uint64_t* k2);
+void launch_gather_tree_keys(bh_ctx* c, const uint32_t* tslot, int n, const float4* pos,
+                             const uint64_t* key_by_slot, float4* tpos, uint64_t* tkey);
 void launch_hash(bh_ctx* c);
 void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc_slot, float4* vel_kick,
-                 float half_dt);
+                 float half_dt, bool batch = false);
 void launch_lookup(bh_ctx* c, uint64_t key, int* out_index);
 void launch_fp32_peak(cudaStream_t st, float* sink, int blocks);
 

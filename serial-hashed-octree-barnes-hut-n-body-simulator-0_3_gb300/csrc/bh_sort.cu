@@ -230,10 +230,16 @@ __global__ __launch_bounds__(kThreads) void k_onesweep(const uint64_t* __restric
 
 int sort_max_tiles(size_t n) { return (int)((n + kTile - 1) / kTile); }
 
+// Function attributes set once per process, before any stream capture.
+void sort_init() {
+  cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(OnesweepSmem));
+}
+
 // Sorts (keys_in, vals_in) stably by the full 64-bit key. The result lands in keys_in /
 // vals_in (an even number of passes); the *_tmp buffers are scratch of the same size.
 void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t* keys_tmp, uint32_t* vals_tmp,
-                      int n, cudaStream_t st, uint64_t** keys_out, uint32_t** vals_out) {
+                      int n, cudaStream_t st, uint64_t** keys_out, uint32_t** vals_out, int first_pass,
+                      int npasses) {
   *keys_out = keys_in;
   *vals_out = vals_in;
   if (n <= 1) return;
@@ -247,14 +253,14 @@ void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t*
   cudaMemsetAsync(c->sort.lookback, 0, sizeof(uint32_t) * (size_t)kPasses * tiles * kRadix, st);
   cudaMemsetAsync(c->sort.tile_ctr, 0, sizeof(uint32_t) * kPasses, st);
   int hblocks = (int)min((long long)152 * 4, ((long long)n + kThreads * 8 - 1) / (kThreads * 8));
-  c->launches += 2 + kPasses;
+  c->launches += 2 + npasses;
   k_hist<<<hblocks, kThreads, 0, st>>>(keys_in, n, c->sort.hist);
   k_hist_scan<<<kPasses, kRadix, 0, st>>>(c->sort.hist);
   uint64_t* ka = keys_in;
   uint32_t* va = vals_in;
   uint64_t* kb = keys_tmp;
   uint32_t* vb = vals_tmp;
-  for (int p = 0; p < kPasses; ++p) {
+  for (int p = first_pass; p < first_pass + npasses; ++p) {
     k_onesweep<<<tiles, kThreads, sizeof(OnesweepSmem), st>>>(ka, va, kb, vb, n, 8 * p, c->sort.hist + p * kRadix,
                                                               c->sort.lookback + (size_t)p * tiles * kRadix,
                                                               c->sort.tile_ctr + p, c->err);

@@ -205,13 +205,15 @@ __global__ void k_set_geom(Geom* __restrict__ g, double c0, double c1, double c2
 // keys, gathers, leapfrog
 // ---------------------------------------------------------------------------------------
 
+// body_sys (optional): system of each body; each system then uses its own geometry
+// sys_geom[body_sys[i]] (batched ensembles), otherwise the single geometry *g.
 __global__ __launch_bounds__(kThreads) void k_morton(const float4* __restrict__ pos, int n,
-                                                     const Geom* __restrict__ g, uint64_t* __restrict__ keys,
-                                                     uint32_t* __restrict__ idx) {
+                                                     const Geom* __restrict__ g, const uint16_t* __restrict__ body_sys,
+                                                     uint64_t* __restrict__ keys, uint32_t* __restrict__ idx) {
   int i = blockIdx.x * kThreads + threadIdx.x;
   if (i >= n) return;
-  const double S = g->size, frac = g->frac;
-  keys[i] = morton_key(pos[i], S, frac);
+  const Geom& gg = body_sys ? g[body_sys[i]] : *g;
+  keys[i] = morton_key(pos[i], gg.size, gg.frac);
   idx[i] = (uint32_t)i;
 }
 
@@ -240,8 +242,8 @@ __global__ __launch_bounds__(kThreads) void k_gather(const uint32_t* __restrict_
 __global__ __launch_bounds__(kThreads) void k_gather_kd_treekey(
     const uint32_t* __restrict__ perm, int n, const float4* __restrict__ pin, const float4* __restrict__ vin,
     const float4* __restrict__ acc, int acc_follows_body, float dt, float half_dt, const Geom* __restrict__ g,
-    float4* __restrict__ pout, float4* __restrict__ vout, uint64_t* __restrict__ tkeys,
-    uint32_t* __restrict__ tidx) {
+    const uint16_t* __restrict__ body_sys, float4* __restrict__ pout, float4* __restrict__ vout,
+    uint64_t* __restrict__ tkeys, uint32_t* __restrict__ tidx) {
   int j = blockIdx.x * kThreads + threadIdx.x;
   if (j >= n) return;
   uint32_t i = perm[j];
@@ -254,7 +256,8 @@ __global__ __launch_bounds__(kThreads) void k_gather_kd_treekey(
   p.z += v.z * dt;
   pout[j] = p;
   vout[j] = v;
-  tkeys[j] = tree_key(p, *g);
+  // the sort keeps every system in its body range, so slot j's system is body_sys[j]
+  tkeys[j] = tree_key(p, body_sys ? g[body_sys[j]] : *g);
   tidx[j] = (uint32_t)j;
 }
 
@@ -509,16 +512,18 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int
                                                       const float4* __restrict__ tpos,
                                                       const uint32_t* __restrict__ tslot,
                                                       WalkNode* __restrict__ wn, NodeUp* __restrict__ nf,
-                                                      const Geom* __restrict__ g, const uint32_t* __restrict__ err,
-                                                      Counters* __restrict__ ctr) {
+                                                      const Geom* __restrict__ g, const uint16_t* __restrict__ body_sys,
+                                                      const uint32_t* __restrict__ err, Counters* __restrict__ ctr) {
   if (*err & kErrNodes) return;
   const int lo = level_bounds[d], hi = level_bounds[d + 1];
   if (hi <= lo) return;
-  const double edge = ldexp(g->tedge, -d);
-  const float s2 = (float)(edge * edge);
+  const double edge0 = ldexp(g->tedge, -d);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&ctr->max_depth, (unsigned)d);
   for (int node = lo + blockIdx.x * kThreads + threadIdx.x; node < hi; node += gridDim.x * kThreads) {
     const int4 link = wn[node].link;
+    // batched ensembles: the node's system (that of its first body) sets the root edge
+    const double edge = body_sys ? ldexp(g[body_sys[link.z]].tedge, -d) : edge0;
+    const float s2 = (float)(edge * edge);
     FF mass = {0.f, 0.f}, com[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     float q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     uint32_t min_rank = 0xffffffffu;
@@ -688,6 +693,112 @@ __global__ __launch_bounds__(kThreads) void k_fp32_peak(float* sink, int iters) 
   if (r == 12345.678f) sink[0] = r;  // keeps the loop alive; never true for these inputs
 }
 
+// ---------------------------------------------------------------------------------------
+// batched ensembles: system s owns the fixed body range [off[s], off[s + 1])
+// ---------------------------------------------------------------------------------------
+
+// OctantBounds of every system, one block per system: FP64 sums in a fixed order (thread
+// stride, then a fixed tree), FP32 maxima of |p|, then the same centre / size / geometry
+// formulas as k_bounds_final.
+__global__ __launch_bounds__(kThreads) void k_batch_bounds(const float4* __restrict__ pos,
+                                                           const uint32_t* __restrict__ off, double edge_factor,
+                                                           Geom* __restrict__ sys_geom) {
+  const int s = blockIdx.x;
+  const int b0 = (int)off[s], b1 = (int)off[s + 1];
+  double sx = 0, sy = 0, sz = 0;
+  float mx = 0.f, my = 0.f, mz = 0.f;
+  for (int i = b0 + threadIdx.x; i < b1; i += kThreads) {
+    const float4 p = pos[i];
+    sx = __dadd_rn(sx, (double)p.x);
+    sy = __dadd_rn(sy, (double)p.y);
+    sz = __dadd_rn(sz, (double)p.z);
+    mx = fmaxf(mx, fabsf(p.x));
+    my = fmaxf(my, fabsf(p.y));
+    mz = fmaxf(mz, fabsf(p.z));
+  }
+  __shared__ double sh[6][kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sx = __dadd_rn(sx, __shfl_down_sync(0xffffffffu, sx, o));
+    sy = __dadd_rn(sy, __shfl_down_sync(0xffffffffu, sy, o));
+    sz = __dadd_rn(sz, __shfl_down_sync(0xffffffffu, sz, o));
+    mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    my = fmaxf(my, __shfl_down_sync(0xffffffffu, my, o));
+    mz = fmaxf(mz, __shfl_down_sync(0xffffffffu, mz, o));
+  }
+  if (lane == 0) {
+    sh[0][w] = sx;
+    sh[1][w] = sy;
+    sh[2][w] = sz;
+    sh[3][w] = mx;
+    sh[4][w] = my;
+    sh[5][w] = mz;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double c[3], m[3];
+  for (int a = 0; a < 3; ++a) {
+    c[a] = sh[a][0];
+    m[a] = sh[3 + a][0];
+    for (int k = 1; k < kThreads / 32; ++k) {
+      c[a] = __dadd_rn(c[a], sh[a][k]);
+      m[a] = fmax(m[a], sh[3 + a][k]);
+    }
+  }
+  const double nn = (double)(b1 - b0);
+  if (nn != 0) {
+    const double inv = __ddiv_rn(1.0, nn);
+    for (int a = 0; a < 3; ++a) c[a] = __dmul_rn(c[a], inv);
+  }
+  double S = 0;
+  for (int a = 0; a < 3; ++a) {
+    const double v = __dsub_rn(m[a], c[a]);
+    if (v > S) S = v;
+  }
+  Geom& g = sys_geom[s];
+  for (int a = 0; a < 3; ++a) g.center[a] = c[a];
+  g.size = S;
+  g.frac = __ddiv_rn(2097152.0, __dmul_rn(2.0, S));
+  fill_tree_geom(g, c, __dmul_rn(S, edge_factor));
+}
+
+// Secondary sort key: the system of the body each sorted element came from. A stable sort of
+// the key-sorted elements by it groups them back into their systems, in key order.
+__global__ __launch_bounds__(kThreads) void k_sys_keys(const uint32_t* __restrict__ vals, int n,
+                                                       const uint16_t* __restrict__ body_sys,
+                                                       uint64_t* __restrict__ k2) {
+  const int j = blockIdx.x * kThreads + threadIdx.x;
+  if (j < n) k2[j] = (uint64_t)body_sys[vals[j]];
+}
+
+// Tree-order positions and tree keys of a batched ensemble: the (system, key) sort leaves the
+// permutation in tslot, the keys themselves are gathered from their per-slot copy.
+__global__ __launch_bounds__(kThreads) void k_gather_tree_keys(const uint32_t* __restrict__ tslot, int n,
+                                                               const float4* __restrict__ pos,
+                                                               const uint64_t* __restrict__ key_by_slot,
+                                                               float4* __restrict__ tpos,
+                                                               uint64_t* __restrict__ tkey) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t s = tslot[i];
+  tpos[i] = pos[s];
+  tkey[i] = key_by_slot[s];
+}
+
+// One root per system at depth 0, in system order.
+__global__ void k_tree_init_batch(int nsys, const uint32_t* __restrict__ off, uint64_t* __restrict__ nkey,
+                                  int2* __restrict__ nrange, int* __restrict__ level_bounds,
+                                  uint32_t* __restrict__ level_tile_ctr) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nsys) {
+    nkey[t] = 1ull;
+    nrange[t] = make_int2((int)off[t], (int)(off[t + 1] - off[t]));
+  }
+  if (t < kLevels) level_tile_ctr[t] = 0;
+  if (t <= kLevels + 1) level_bounds[t] = (t == 0) ? 0 : (t == 1 ? nsys : -1);
+}
+
 inline int grid_for(long long n) { return (int)((n + kThreads - 1) / kThreads); }
 
 }  // namespace
@@ -708,9 +819,11 @@ void launch_set_geom(bh_ctx* c, const double center[3], double size, const doubl
                                       tcenter[2], tedge);
 }
 
-void launch_morton(bh_ctx* c, const float4* pos, int n, uint64_t* keys, uint32_t* idx) {
+void launch_morton(bh_ctx* c, const float4* pos, int n, uint64_t* keys, uint32_t* idx, bool batch) {
   if (n > 0) c->launches += 1;
-  if (n > 0) k_morton<<<grid_for(n), kThreads, 0, c->stream>>>(pos, n, c->geom, keys, idx);
+  if (n > 0)
+    k_morton<<<grid_for(n), kThreads, 0, c->stream>>>(pos, n, batch ? c->sys_geom : c->geom,
+                                                       batch ? c->body_sys : nullptr, keys, idx);
 }
 
 void launch_treekey(bh_ctx* c, const float4* pos, int n, uint64_t* tkeys, uint32_t* tidx) {
@@ -726,11 +839,12 @@ void launch_gather(bh_ctx* c, const uint32_t* perm, int n, const float4* pin, co
 
 void launch_gather_kd_treekey(bh_ctx* c, const uint32_t* perm, int n, const float4* pin, const float4* vin,
                               const float4* acc, int acc_follows_body, float dt, float4* pout, float4* vout,
-                              uint64_t* tkeys, uint32_t* tidx) {
+                              uint64_t* tkeys, uint32_t* tidx, bool batch) {
   if (n > 0) c->launches += 1;
   if (n > 0)
-    k_gather_kd_treekey<<<grid_for(n), kThreads, 0, c->stream>>>(perm, n, pin, vin, acc, acc_follows_body, dt,
-                                                                  0.5f * dt, c->geom, pout, vout, tkeys, tidx);
+    k_gather_kd_treekey<<<grid_for(n), kThreads, 0, c->stream>>>(
+        perm, n, pin, vin, acc, acc_follows_body, dt, 0.5f * dt, batch ? c->sys_geom : c->geom,
+        batch ? c->body_sys : nullptr, pout, vout, tkeys, tidx);
 }
 
 void launch_kick_drift(bh_ctx* c, float4* pos, float4* vel, const float4* acc, int n, float dt, int drift) {
@@ -743,9 +857,13 @@ void launch_gather_tree(bh_ctx* c, const uint32_t* tslot, int n, const float4* p
   if (n > 0) k_gather_tree<<<grid_for(n), kThreads, 0, c->stream>>>(tslot, n, pos, tpos);
 }
 
-void launch_build(bh_ctx* c, int n, int leaf_cap) {
+void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
   c->launches += 1 + kLevels;
-  k_tree_init<<<1, 64, 0, c->stream>>>(n, c->nkey, c->nrange, c->level_bounds, c->level_tile_ctr);
+  if (batch)
+    k_tree_init_batch<<<(max(c->nsys, kLevels + 2) + 255) / 256, 256, 0, c->stream>>>(
+        c->nsys, c->sys_off, c->nkey, c->nrange, c->level_bounds, c->level_tile_ctr);
+  else
+    k_tree_init<<<1, 64, 0, c->stream>>>(n, c->nkey, c->nrange, c->level_bounds, c->level_tile_ctr);
   const int max_tiles = c->lb_level_tiles;
   cudaMemsetAsync(c->lb_level, 0, sizeof(uint32_t) * (size_t)kLevels * max_tiles, c->stream);
   const int grid = 152 * 4;
@@ -755,14 +873,33 @@ void launch_build(bh_ctx* c, int n, int leaf_cap) {
                                               c->lb_level + (size_t)d * max_tiles, (long long)c->node_cap, c->err);
 }
 
-void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode) {
+void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode, bool batch) {
   (void)leaf_cap;
   if (n <= 0) return;
   const int grid = 152 * 8;
   c->launches += kLevels;
   for (int d = kMaxDepth; d >= 0; --d)
     k_upsweep<<<grid, kThreads, 0, c->stream>>>(d, mode, c->level_bounds, c->tpos, c->tslot, c->wnode, c->nup,
-                                                c->geom, c->err, c->counters);
+                                                batch ? c->sys_geom : c->geom, batch ? c->body_sys : nullptr,
+                                                c->err, c->counters);
+}
+
+void launch_batch_bounds(bh_ctx* c, const float4* pos, double edge_factor) {
+  c->launches += 1;
+  k_batch_bounds<<<c->nsys, kThreads, 0, c->stream>>>(pos, c->sys_off, edge_factor, c->sys_geom);
+}
+
+void launch_gather_tree_keys(bh_ctx* c, const uint32_t* tslot, int n, const float4* pos,
+                             const uint64_t* key_by_slot, float4* tpos, uint64_t* tkey) {
+  if (n <= 0) return;
+  c->launches += 1;
+  k_gather_tree_keys<<<grid_for(n), kThreads, 0, c->stream>>>(tslot, n, pos, key_by_slot, tpos, tkey);
+}
+
+void launch_sys_keys(bh_ctx* c, const uint32_t* vals, int n, uint64_t* k2) {
+  if (n <= 0) return;
+  c->launches += 1;
+  k_sys_keys<<<grid_for(n), kThreads, 0, c->stream>>>(vals, n, c->body_sys, k2);
 }
 
 void launch_hash(bh_ctx* c) {

@@ -182,6 +182,7 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
                                                    const uint32_t* __restrict__ tslot, int n, float theta2,
                                                    float eps2, float4* __restrict__ acc_slot,
                                                    float4* __restrict__ vel_kick, float half_dt,
+                                                   const int4* __restrict__ groups, int ngroups_table,
                                                    Counters* __restrict__ ctr, uint32_t* __restrict__ err) {
   __shared__ WarpSmem smem[kWarps];
   const int lane = threadIdx.x & 31;
@@ -189,8 +190,10 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
   const uint32_t lt_mask = lanebit - 1u;
   WarpSmem& s = smem[threadIdx.x >> 5];
   if (*((volatile uint32_t*)err) & (kErrNodes | kErrTimeout)) return;
-  const int ngroups = (n + 31) >> 5;
-  const int4 root_link = __ldg(&nodes[0].link);
+  // work items: groups of up to 32 consecutive bodies (tree order) under one root. Without a
+  // group table, group g is bodies [32 g, 32 g + 32) of the single tree rooted at node 0;
+  // batched ensembles pass (first body, body count, root node) per group.
+  const int ngroups = groups ? ngroups_table : (n + 31) >> 5;
   const float acc_scale = theta2 * (1.f - kMacMargin);
   const float open_scale = theta2 * (1.f + kMacMargin);
   unsigned long long tot_cell = 0, tot_pt = 0, ev_cell = 0, ev_pt = 0;  // ev_*: warp-uniform
@@ -201,9 +204,20 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
     if (lane == 0) g = (int)atomicAdd(&ctr->group_next, 1u);
     g = __shfl_sync(0xffffffffu, g, 0);
     if (g >= ngroups) break;
-    const int gbase = g * 32;
+    int gbase, gcount, root;
+    if (groups) {
+      const int4 gr = __ldg(groups + g);
+      gbase = gr.x;
+      gcount = gr.y;
+      root = gr.z;
+    } else {
+      gbase = g * 32;
+      gcount = min(32, n - gbase);
+      root = 0;
+    }
+    const int4 root_link = __ldg(&nodes[root].link);
     const int i = gbase + lane;
-    const bool valid = i < n;
+    const bool valid = lane < gcount;
     const float4 p = __ldg(tpos + (valid ? i : gbase));
     const uint32_t active = __ballot_sync(0xffffffffu, valid);
     // bounding box of the group's bodies
@@ -482,16 +496,27 @@ int walk_grid() {
 }
 
 template <bool kQuad, bool kSelf>
-void launch_walk_t(bh_ctx* c, int n, float theta2, float eps2, float4* acc_slot, float4* vel_kick, float half_dt) {
-  const int grid = min(walk_grid<kQuad, kSelf>(), (n + 31) / 32 / kWarps + 1);
+void launch_walk_t(bh_ctx* c, int n, float theta2, float eps2, float4* acc_slot, float4* vel_kick, float half_dt,
+                   bool batch) {
+  const int ngroups = batch ? c->ngroups : (n + 31) / 32;
+  const int grid = min(walk_grid<kQuad, kSelf>(), ngroups / kWarps + 1);
   k_walk<kQuad, kSelf><<<grid, kThreads, 0, c->stream>>>(c->wnode, c->tpos, c->tslot, n, theta2, eps2, acc_slot,
-                                                         vel_kick, half_dt, c->counters, c->err);
+                                                         vel_kick, half_dt, batch ? c->groups : nullptr,
+                                                         c->ngroups, c->counters, c->err);
 }
 
 }  // namespace
 
+// Occupancy queries done once per process, before any stream capture.
+void walk_init() {
+  walk_grid<true, true>();
+  walk_grid<true, false>();
+  walk_grid<false, true>();
+  walk_grid<false, false>();
+}
+
 void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc_slot, float4* vel_kick,
-                 float half_dt) {
+                 float half_dt, bool batch) {
   if (n <= 0) return;
   cudaMemsetAsync(&c->counters->group_next, 0, sizeof(unsigned), c->stream);
   c->launches += 1;
@@ -500,14 +525,14 @@ void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc
   const bool self = !(eps2 > 0.f);
   if (quad) {
     if (self)
-      launch_walk_t<true, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt);
+      launch_walk_t<true, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
     else
-      launch_walk_t<true, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt);
+      launch_walk_t<true, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
   } else {
     if (self)
-      launch_walk_t<false, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt);
+      launch_walk_t<false, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
     else
-      launch_walk_t<false, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt);
+      launch_walk_t<false, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
   }
 }
 

@@ -1,0 +1,72 @@
+"""Batched ensembles: one bh_batch_step over many systems against the plain path per system.
+
+Each system of the ensemble must evolve exactly as it does alone through bh_step: same
+permutation (the system's own Morton order inside its body range), and positions, velocities
+and accelerations equal up to FP32 rounding (the only difference is the summation order of the
+system's FP64 bounds centre)."""
+import numpy as np
+import pytest
+
+from oracle.oracle import relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def ensemble(bh, nsys, seed, nmin=40, nmax=3000):
+    rng = np.random.default_rng(seed)
+    sizes = np.round(np.exp(rng.uniform(np.log(nmin), np.log(nmax), nsys))).astype(int)
+    pos, vel = [], []
+    for s, n in enumerate(sizes):
+        p, v = bh.plummer(seed * 1000 + s, int(n))
+        v[:, 3] = np.arange(n, dtype=np.float32)  # body id rides in the unused velocity lane
+        pos.append(p)
+        vel.append(v)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint32)
+    return np.concatenate(pos), np.concatenate(vel), off
+
+
+@pytest.mark.parametrize("leaf,mode", [(8, 1), (1, 0)])
+def test_batch_step_matches_plain_per_system(bh, leaf, mode):
+    pm, vel, off = ensemble(bh, 37, 5)
+    prm = bh.default_params(theta=0.6, eps=0.01, dt=1e-3, leaf_capacity=leaf, multipole=mode, edge_factor=2.0)
+    nsteps = 3
+    with bh.Simulation(len(pm)) as sim:
+        sim.batch_set(pm, vel, off)
+        st = sim.batch_step(prm, nsteps)
+        assert st.steps == nsteps and st.error_flags == 0
+        bp, bv, ba = sim.get_bodies()
+    worst = 0.0
+    with bh.Simulation(int(np.diff(off).max())) as one:
+        for s in range(len(off) - 1):
+            a, b = off[s], off[s + 1]
+            one.set_bodies(pm[a:b], vel[a:b])
+            one.step(prm, nsteps)
+            p, v, acc = one.get_bodies()
+            assert np.array_equal(bv[a:b, 3], v[:, 3]), f"system {s}: permutation differs"
+            assert np.allclose(bp[a:b, :3], p[:, :3], rtol=0, atol=1e-6)
+            assert np.allclose(bv[a:b, :3], v[:, :3], rtol=0, atol=1e-6)
+            worst = max(worst, float(relerr(ba[a:b], acc).max()))
+    assert worst <= 1e-5
+
+
+def test_batch_then_plain_reuse(bh):
+    """A context switches between an ensemble and a single system without stale state."""
+    pm, vel, off = ensemble(bh, 5, 9, 100, 400)
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=4)
+    with bh.Simulation(len(pm)) as sim:
+        sim.batch_set(pm, vel, off)
+        sim.batch_step(prm, 2)
+        sim.set_bodies(pm[: off[1]], vel[: off[1]])
+        st = sim.step(prm, 1)
+        assert st.error_flags == 0
+        sim.batch_set(pm, vel, off)
+        st = sim.batch_step(prm, 1)
+        assert st.steps == 1
+
+
+def test_batch_set_rejects_bad_offsets(bh):
+    pm, vel = bh.plummer(1, 100)
+    with bh.Simulation(100) as sim:
+        for off in ([0, 50, 50, 100], [1, 100], [0, 60, 40, 100]):
+            with pytest.raises(bh.BHError):
+                sim.batch_set(pm, vel, np.array(off, np.uint32))
