@@ -494,13 +494,112 @@ def run_ensemble(args, dist):
         print(json.dumps(line), flush=True)
 
 
+ADJOINT = dict(n=65536, nsteps=200, every=20, theta=0.5, eps=0.01, leaf=8, dt=1e-3, edge=1.0, seed=1, tseed=2,
+               desc="Plummer sphere N=65536 (seed 1), 200 KDK steps, dt=1e-3, theta=0.5, eps=0.01, leaf 8, "
+                    "quadrupole; loss = mean squared distance of final positions to the final positions of a run "
+                    "with lognormal(0.1) mass factors (seed 2); checkpoints every 20 steps")
+
+
+def run_adjoint(args, dist):
+    """Reverse mode: a step is one gradient of the loss over the whole 200-step trajectory
+    (bh_adjoint_forward with checkpoints + bh_step_backward with recomputation). Beside it, the
+    plain forward path (bh_step) over the same 200 steps, so the backward/forward cost ratio is
+    measured in the same run."""
+    import __graft_entry__
+
+    bh = __graft_entry__.package()
+    bh.load()
+    a = ADJOINT
+    n, ns = a["n"], a["nsteps"]
+    pm, vel = bh.plummer(a["seed"], n)
+    prm = bh.default_params(theta=a["theta"], eps=a["eps"], dt=a["dt"], leaf_capacity=a["leaf"],
+                            multipole=bh.BH_MULTIPOLE_QUADRUPOLE, edge_factor=a["edge"], acc_follows_body=1)
+    sim = bh.Simulation(n)
+    tpm = pm.copy()
+    tpm[:, 3] *= np.random.default_rng(a["tseed"]).lognormal(0.0, 0.1, n).astype(np.float32)
+    sim.set_bodies(tpm, vel)
+    sim.adjoint_forward(prm, ns, ns)
+    target = sim.get_bodies()[0][:, :3].copy()
+
+    def gradient(timed):
+        sim.set_bodies(pm, vel)
+        if timed:
+            sim.flush_l2()
+        f = sim.adjoint_forward(prm, ns, a["every"])
+        p = sim.get_bodies()[0]
+        dl = (2.0 * (p[:, :3] - target) / n).astype(np.float32)
+        if timed:
+            sim.flush_l2()
+        g = sim.step_backward(dl, None, stats=True)
+        return f, g[3], float(np.mean(np.sum((p[:, :3] - target) ** 2, axis=1)))
+
+    for _ in range(args.warmup):
+        gradient(False)
+    fwd, bwd, launches = [], [], 0
+    dist.barrier()
+    with ClockSampler(int(os.environ.get("BH_GPU_INDEX", "0"))) as clocks:
+        for _ in range(args.steps):
+            f, b, loss = gradient(True)
+            fwd.append(f.ms_step)
+            bwd.append(b.ms_step)
+            launches += f.kernel_launches + b.kernel_launches
+        # the plain forward path over the same trajectory length
+        plain = []
+        for _ in range(max(2, args.steps)):
+            sim.set_bodies(pm, vel)
+            sim.flush_l2()
+            plain.append(sim.step(prm, ns).ms_step)
+    total_ms = dist.max(sum(fwd) + sum(bwd))
+    value = dist.sum(n * ns * args.steps) / (total_ms * 1e-3)
+    # end to end through the C ABI: host state in, loss cotangent in, gradients out
+    pp, pv, pd = bh.PinnedArray((n, 4)), bh.PinnedArray((n, 4)), bh.PinnedArray((n, 4))
+    pp.array[:] = pm
+    pv.array[:] = vel
+    e2e = []
+    for _ in range(2):
+        sim.event_record(0)
+        sim.set_bodies(pp.array, pv.array)
+        sim.adjoint_forward(prm, ns, a["every"], stats=False)
+        p = sim.get_bodies()[0]
+        pd.array[:, :3] = 2.0 * (p[:, :3] - target) / n
+        sim.step_backward(pd.array, None)
+        sim.event_record(1)
+        e2e.append(sim.event_elapsed_ms(0, 1))
+    for x in (pp, pv, pd):
+        x.free()
+    sim.close()
+    plain_ms = statistics.median(plain)
+    if dist.rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "body-steps/s (differentiated)", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "impl": "ours",
+                "config": {"workload": "adjoint-64k", "bodies": n, "kdk_steps": ns, "checkpoint_every": a["every"],
+                           "desc": a["desc"],
+                           "timing": "a step = one gradient over the 200-step trajectory; CUDA events around "
+                                     "bh_adjoint_forward and bh_step_backward; L2 flushed before each"},
+                "forward_ms": statistics.median(fwd), "backward_ms": statistics.median(bwd),
+                "plain_forward_ms": plain_ms,
+                "backward_over_forward": statistics.median(bwd) / plain_ms,
+                "gradient_over_forward": (statistics.median(fwd) + statistics.median(bwd)) / plain_ms,
+                "loss": loss,
+                "gradient_checks": "tests/test_gpu_adjoint.py (FP64 frozen-list central differences, FP64 "
+                                   "direct-sum adjoint)",
+                "e2e": {"value": n * ns / (statistics.median(e2e) * 1e-3), "unit": "body-steps/s (differentiated)",
+                        "h2d_bytes_per_step": 48 * n, "d2h_bytes_per_step": 32 * n + 36 * n,
+                        "ms_per_step": statistics.median(e2e)},
+                "gpu_launches": launches, "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="plummer-4m", choices=sorted(WORKLOADS) + ["ensemble-4096"])
+    ap.add_argument("--workload", default="plummer-4m",
+                    choices=sorted(WORKLOADS) + ["ensemble-4096", "adjoint-64k"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--cpu-walk-sample", type=int, default=16384)
@@ -509,8 +608,17 @@ def main():
     if args.warmup < 3:
         log("warning: fewer than 3 warm-up steps")
     dist = Dist()
+    if args.workload in ("ensemble-4096", "adjoint-64k") and args.impl == "reference":
+        if dist.rank == 0:
+            why = ("the reference has no batched mode" if args.workload == "ensemble-4096"
+                   else "the reference has no reverse mode")
+            print(json.dumps({"impl": "reference", "unavailable": why}), flush=True)
+        return
     if args.workload == "ensemble-4096":
         run_ensemble(args, dist)
+        return
+    if args.workload == "adjoint-64k":
+        run_adjoint(args, dist)
         return
     w = WORKLOADS[args.workload]
     if args.impl == "reference":

@@ -55,7 +55,8 @@ typedef enum bh_status {
   BH_ERR_OVERFLOW_NODES = 6,  /* node arena too small; bh_step grows it and retries itself */
   BH_ERR_TIMEOUT = 7,         /* a bounded device-side wait gave up (device flag) */
   BH_ERR_NO_TREE = 8,         /* bh_force / bh_tree_* called before bh_build */
-  BH_ERR_NOT_FOUND = 9        /* bh_node_lookup: no node with that key */
+  BH_ERR_NOT_FOUND = 9,       /* bh_node_lookup: no node with that key */
+  BH_ERR_OVERFLOW_TAPE = 10   /* adjoint interaction tape too small; bh_step_backward grows it itself */
 } bh_status;
 
 typedef enum bh_multipole_mode {
@@ -230,6 +231,24 @@ bh_status bh_measure_fp32_peak(bh_ctx* ctx, double* tflops);
 #define BH_SORT_STATIC_MAX_KEYS 65536
 bh_status bh_sort_keys_static(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                               uint32_t* vals_out, size_t n, void* stream, uint32_t* status_out);
+
+/* Differentiable trajectory (reverse mode). The reference has no counterpart: it only
+ * integrates forward (Simulation::run, src/Simulation.cpp). bh_adjoint_forward integrates
+ * nsteps kick-drift-kick steps of the quadrupole tree force from the uploaded state (bodies
+ * keep their upload order, no Morton reordering; a(x_0) is computed first from a tree over
+ * x_0), storing (x, v, a) every checkpoint_every steps. bh_step_backward then takes the
+ * gradients of a scalar loss with respect to the final positions and velocities (float4 per
+ * body, w ignored; either may be null = zero) and returns its gradients with respect to the
+ * initial positions, velocities (float4, w = 0) and masses (one float per body); any output
+ * may be null. The tree walks' opening decisions are held fixed (each segment is re-run from
+ * its checkpoint with the walk's interaction lists recorded), so the gradient is that of the
+ * piecewise-smooth map the forward pass followed. Requires multipole = quadrupole and eps > 0;
+ * all host buffers are the caller's. After bh_step_backward the bodies are in the state the
+ * forward pass ended in, and further backward calls with other loss gradients are allowed. */
+bh_status bh_adjoint_forward(bh_ctx* ctx, const bh_params* params, int nsteps, int checkpoint_every,
+                             bh_stats* stats);
+bh_status bh_step_backward(bh_ctx* ctx, const float* dloss_dpos4, const float* dloss_dvel4, float* grad_pos4,
+                           float* grad_vel4, float* grad_mass, bh_stats* stats);
 
 /* Host-side synthetic initial conditions (set-up time, not the per-step path): a Plummer
  * sphere of n bodies, scale radius a, total mass mtot, shifted to its centre-of-mass frame,

@@ -273,13 +273,34 @@ struct Walker {
   // of LinearHashedOctree::MAC (src/HashedOctree.cpp:872-885), followed by the list sum.
   // Leaves with one body are self-skipped by exact position (:376); bucket leaves are summed
   // over their members with the same position test.
+  struct Item {
+    const Node* nd;  // a node (cell, or single-body leaf), or null for a member body of an opened bucket leaf
+    int32_t body;
+  };
   void body(const double p[3], double acc[3], long* n_cell, long* n_p2p) const {
-    struct Item {
-      const Node* nd;
-      int32_t body;
-    };
-    std::vector<const Node*> stack;
     std::vector<Item> list;
+    gather(p, list);
+    acc[0] = acc[1] = acc[2] = 0;
+    long nc = 0, np = 0;
+    for (const Item& it : list) {
+      if (it.nd) {
+        interact(p, it.nd->com, it.nd->mass, it.nd->n, mode == 1 ? it.nd->q : nullptr, eps2, acc);
+        if (it.nd->n > 1)
+          ++nc;
+        else
+          ++np;
+      } else {
+        interact(p, pos3 + 3 * it.body, mass[it.body], 1, nullptr, eps2, acc);
+        ++np;
+      }
+    }
+    *n_cell = nc;
+    *n_p2p = np;
+  }
+  // The interaction list of the body at p, in the walk's order.
+  void gather(const double p[3], std::vector<Item>& list) const {
+    std::vector<const Node*> stack;
+    list.clear();
     stack.push_back(&nodes.at(1));
     const double th2 = theta * theta;
     while (!stack.empty()) {
@@ -316,22 +337,6 @@ struct Walker {
         }
       }
     }
-    acc[0] = acc[1] = acc[2] = 0;
-    long nc = 0, np = 0;
-    for (const Item& it : list) {
-      if (it.nd) {
-        interact(p, it.nd->com, it.nd->mass, it.nd->n, mode == 1 ? it.nd->q : nullptr, eps2, acc);
-        if (it.nd->n > 1)
-          ++nc;
-        else
-          ++np;
-      } else {
-        interact(p, pos3 + 3 * it.body, mass[it.body], 1, nullptr, eps2, acc);
-        ++np;
-      }
-    }
-    *n_cell = nc;
-    *n_p2p = np;
   }
   std::unordered_map<const Node*, uint64_t> keys;
   uint64_t node_key(const Node* nd) const { return keys.at(nd); }
@@ -653,6 +658,264 @@ int orc_time_sample(const double* pos3, const double* mass, size_t n, const doub
   *build_s = (t1 - t0) + (t1b - t1);
   *walk_s = t2 - t1b;
   return 0;
+}
+
+}  // extern "C"
+
+// ---- Differentiable trajectory (checker for bh_adjoint_forward / bh_step_backward) ----
+// The reference has no reverse mode; these follow the library's differentiable path: bodies keep
+// their order, a(x_0) comes from a tree over x_0 with the bounds of x_0, step n builds its tree
+// over x_{n+1} with the bounds of x_n (root edge = S * edge_factor), quadrupole multipoles, and
+// the interaction lists of the forward pass are held fixed.
+namespace {
+
+// Interaction lists of one force evaluation, held fixed for replays.
+struct FrozenForce {
+  std::vector<uint32_t> cell_off{0};  // cell c: member bodies cell_mem[cell_off[c] .. cell_off[c + 1])
+  std::vector<uint32_t> cell_mem;
+  std::vector<uint32_t> off;          // body i: entries ent[off[i] .. off[i + 1])
+  std::vector<int32_t> ent;           // >= 0: point source body; < 0: cell -(c + 1)
+};
+
+struct Frozen {
+  size_t n = 0;
+  double dt = 0, eps = 0;
+  int nsteps = 0;
+  std::vector<FrozenForce> f;  // a(x_0), a(x_1), ..., a(x_nsteps)
+};
+
+void collect_members(const NodeMap& nodes, uint64_t key, std::vector<uint32_t>& out) {
+  const Node& nd = nodes.at(key);
+  if (nd.child == 0) {
+    out.insert(out.end(), nd.members.begin(), nd.members.end());
+    return;
+  }
+  for (int o = 0; o < 8; ++o)
+    if (nd.child & (1u << o)) collect_members(nodes, (key << 3) | (uint64_t)o, out);
+}
+
+// Tree over pos (root centre c, edge), quadrupole upsweep, every body's interaction list.
+void record_force(const double* pos3, const double* mass, size_t n, const double c[3], double edge, int L,
+                  double theta, double eps, int nthreads, FrozenForce& ff) {
+  NodeMap nodes;
+  insert_all(nodes, pos3, mass, n, c, edge, L < 1 ? 1 : L);
+  upsweep(nodes, 1, pos3, mass);
+  Walker w{nodes, pos3, mass, theta, eps * eps, 1, {}};
+  w.keys.reserve(nodes.size());
+  for (auto& kv : nodes) w.keys[&kv.second] = kv.first;
+  std::vector<std::vector<Walker::Item>> lists(n);
+  for_threads(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) w.gather(pos3 + 3 * i, lists[i]);
+  });
+  std::unordered_map<const Node*, int32_t> cell_id;
+  ff = FrozenForce();
+  ff.off.assign(n + 1, 0);
+  for (size_t i = 0; i < n; ++i) {
+    ff.off[i] = (uint32_t)ff.ent.size();
+    for (const Walker::Item& it : lists[i]) {
+      if (!it.nd) {
+        ff.ent.push_back(it.body);
+      } else if (it.nd->n <= 1) {
+        ff.ent.push_back((int32_t)it.nd->members[0]);  // single-body leaf
+      } else {
+        auto f = cell_id.find(it.nd);
+        int32_t id;
+        if (f == cell_id.end()) {
+          id = (int32_t)cell_id.size();
+          cell_id.emplace(it.nd, id);
+          collect_members(nodes, w.node_key(it.nd), ff.cell_mem);
+          ff.cell_off.push_back((uint32_t)ff.cell_mem.size());
+        } else {
+          id = f->second;
+        }
+        ff.ent.push_back(-(id + 1));
+      }
+    }
+  }
+  ff.off[n] = (uint32_t)ff.ent.size();
+}
+
+// Accelerations from frozen lists: each cell's mass, centre of mass and quadrupole are
+// recomputed from its members' current positions.
+void frozen_force(const FrozenForce& ff, const double* pos3, const double* mass, size_t n, double eps2,
+                  int nthreads, double* acc3) {
+  const size_t nc = ff.cell_off.size() - 1;
+  std::vector<double> cm(4 * nc), cq(6 * nc);
+  for_threads(nc, nthreads, [&](size_t b, size_t e) {
+    for (size_t c = b; c < e; ++c) {
+      double m = 0, x[3] = {0, 0, 0};
+      for (uint32_t k = ff.cell_off[c]; k < ff.cell_off[c + 1]; ++k) {
+        const uint32_t j = ff.cell_mem[k];
+        m += mass[j];
+        for (int a = 0; a < 3; ++a) x[a] += mass[j] * pos3[3 * j + a];
+      }
+      for (int a = 0; a < 3; ++a) x[a] /= m;
+      double q[6] = {0, 0, 0, 0, 0, 0};
+      for (uint32_t k = ff.cell_off[c]; k < ff.cell_off[c + 1]; ++k) {
+        const uint32_t j = ff.cell_mem[k];
+        const double rx = pos3[3 * j] - x[0], ry = pos3[3 * j + 1] - x[1], rz = pos3[3 * j + 2] - x[2];
+        const double mj = mass[j], r2 = rx * rx + ry * ry + rz * rz;
+        q[0] += mj * (3 * rx * rx - r2);
+        q[1] += mj * 3 * rx * ry;
+        q[2] += mj * 3 * rx * rz;
+        q[3] += mj * (3 * ry * ry - r2);
+        q[4] += mj * 3 * ry * rz;
+        q[5] += mj * (3 * rz * rz - r2);
+      }
+      cm[4 * c] = x[0];
+      cm[4 * c + 1] = x[1];
+      cm[4 * c + 2] = x[2];
+      cm[4 * c + 3] = m;
+      for (int k = 0; k < 6; ++k) cq[6 * c + k] = q[k];
+    }
+  });
+  for_threads(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      double a[3] = {0, 0, 0};
+      for (uint32_t k = ff.off[i]; k < ff.off[i + 1]; ++k) {
+        const int32_t t = ff.ent[k];
+        if (t >= 0) {
+          interact(pos3 + 3 * i, pos3 + 3 * t, mass[t], 1, nullptr, eps2, a);
+        } else {
+          const size_t c = (size_t)(-t - 1);
+          interact(pos3 + 3 * i, &cm[4 * c], cm[4 * c + 3], 2, &cq[6 * c], eps2, a);
+        }
+      }
+      acc3[3 * i] = a[0];
+      acc3[3 * i + 1] = a[1];
+      acc3[3 * i + 2] = a[2];
+    }
+  });
+}
+
+// KDK trajectory in place on (x, v); records the lists first when `record`.
+void frozen_traj(Frozen& fr, bool record, double* x, double* v, const double* m, double theta, double edge_factor,
+                 int L, int nthreads) {
+  const size_t n = fr.n;
+  const double dt = fr.dt, eps2 = fr.eps * fr.eps;
+  std::vector<double> a(3 * n);
+  double c[3], S;
+  if (record) {
+    fr.f.assign(fr.nsteps + 1, FrozenForce());
+    orc_bounds(x, n, c, &S);
+    record_force(x, m, n, c, S * edge_factor, L, theta, fr.eps, nthreads, fr.f[0]);
+  }
+  frozen_force(fr.f[0], x, m, n, eps2, nthreads, a.data());
+  for (int s = 0; s < fr.nsteps; ++s) {
+    if (record) orc_bounds(x, n, c, &S);
+    orc_kick_drift(x, v, a.data(), n, dt);
+    if (record) record_force(x, m, n, c, S * edge_factor, L, theta, fr.eps, nthreads, fr.f[s + 1]);
+    frozen_force(fr.f[s + 1], x, m, n, eps2, nthreads, a.data());
+    orc_kick(v, a.data(), n, dt);
+  }
+}
+
+// (xb, mb) += vector-Jacobian product of the FP64 direct-sum acceleration at x applied to ab.
+void direct_vjp(const double* x, const double* m, size_t n, double eps2, const double* ab, int nthreads, double* xb,
+                double* mb) {
+  for_threads(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      double gx = 0, gy = 0, gz = 0, gm = 0;
+      const double* ai = ab + 3 * i;
+      for (size_t j = 0; j < n; ++j) {
+        if (j == i) continue;
+        const double dx = x[3 * j] - x[3 * i], dy = x[3 * j + 1] - x[3 * i + 1], dz = x[3 * j + 2] - x[3 * i + 2];
+        const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+        const double ri = 1.0 / std::sqrt(r2);
+        const double w3 = ri * ri * ri, w5 = w3 * ri * ri;
+        // a_i's dependence on x_i (through d = x_j - x_i)
+        const double adi = ai[0] * dx + ai[1] * dy + ai[2] * dz;
+        gx -= m[j] * (w3 * ai[0] - 3 * w5 * adi * dx);
+        gy -= m[j] * (w3 * ai[1] - 3 * w5 * adi * dy);
+        gz -= m[j] * (w3 * ai[2] - 3 * w5 * adi * dz);
+        // a_j's dependence on x_i and m_i (source i, d' = x_i - x_j = -d)
+        const double* aj = ab + 3 * j;
+        const double adj = -(aj[0] * dx + aj[1] * dy + aj[2] * dz);
+        gx += m[i] * (w3 * aj[0] + 3 * w5 * adj * dx);
+        gy += m[i] * (w3 * aj[1] + 3 * w5 * adj * dy);
+        gz += m[i] * (w3 * aj[2] + 3 * w5 * adj * dz);
+        gm += w3 * adj;
+      }
+      xb[3 * i] += gx;
+      xb[3 * i + 1] += gy;
+      xb[3 * i + 2] += gz;
+      mb[i] += gm;
+    }
+  });
+}
+
+}  // namespace
+
+extern "C" {
+
+// Records a trajectory with its interaction lists (returns a handle; pos_out / vel_out get the
+// final state).
+void* orc_frozen_record(const double* pos3, const double* vel3, const double* mass, size_t n, double dt,
+                        double theta, double eps, double edge_factor, int L, int nsteps, int nthreads,
+                        double* pos_out, double* vel_out) {
+  Frozen* fr = new Frozen();
+  fr->n = n;
+  fr->dt = dt;
+  fr->eps = eps;
+  fr->nsteps = nsteps;
+  std::memcpy(pos_out, pos3, 3 * n * sizeof(double));
+  std::memcpy(vel_out, vel3, 3 * n * sizeof(double));
+  frozen_traj(*fr, true, pos_out, vel_out, mass, theta, edge_factor, L, nthreads);
+  return fr;
+}
+
+// Re-runs the recorded trajectory's map (lists held fixed) from another initial state.
+void orc_frozen_run(void* h, const double* pos3, const double* vel3, const double* mass, int nthreads,
+                    double* pos_out, double* vel_out) {
+  Frozen* fr = (Frozen*)h;
+  std::memcpy(pos_out, pos3, 3 * fr->n * sizeof(double));
+  std::memcpy(vel_out, vel3, 3 * fr->n * sizeof(double));
+  frozen_traj(*fr, false, pos_out, vel_out, mass, 0, 1, 1, nthreads);
+}
+
+// Total list entries over all recorded force evaluations (cells and points).
+long orc_frozen_entries(void* h) {
+  long t = 0;
+  for (const FrozenForce& f : ((Frozen*)h)->f) t += (long)f.ent.size();
+  return t;
+}
+
+void orc_frozen_free(void* h) { delete (Frozen*)h; }
+
+// FP64 direct-sum KDK trajectory and its adjoint: gradients with respect to the initial
+// positions, velocities and masses of a loss whose gradients with respect to the final
+// positions and velocities are dl_dx / dl_dv.
+void orc_direct_adjoint(const double* pos3, const double* vel3, const double* mass, size_t n, double dt, double eps,
+                        int nsteps, const double* dl_dx, const double* dl_dv, int nthreads, double* pos_out,
+                        double* vel_out, double* gx, double* gv, double* gm) {
+  const double e2 = eps * eps, h = 0.5 * dt;
+  std::vector<double> xs(3 * n * (size_t)(nsteps + 1)), v(vel3, vel3 + 3 * n), a(3 * n);
+  std::memcpy(xs.data(), pos3, 3 * n * sizeof(double));
+  orc_direct(xs.data(), mass, n, nullptr, n, eps, nthreads, a.data(), nullptr);
+  for (int s = 0; s < nsteps; ++s) {
+    double* x = xs.data() + 3 * n * (size_t)(s + 1);
+    std::memcpy(x, x - 3 * n, 3 * n * sizeof(double));
+    orc_kick_drift(x, v.data(), a.data(), n, dt);
+    orc_direct(x, mass, n, nullptr, n, eps, nthreads, a.data(), nullptr);
+    orc_kick(v.data(), a.data(), n, dt);
+  }
+  std::memcpy(pos_out, xs.data() + 3 * n * (size_t)nsteps, 3 * n * sizeof(double));
+  std::memcpy(vel_out, v.data(), 3 * n * sizeof(double));
+  std::vector<double> xb(3 * n, 0.0), vb(3 * n, 0.0), carry(3 * n, 0.0), ab(3 * n), mb(n, 0.0);
+  if (dl_dx) std::memcpy(xb.data(), dl_dx, 3 * n * sizeof(double));
+  if (dl_dv) std::memcpy(vb.data(), dl_dv, 3 * n * sizeof(double));
+  for (int s = nsteps - 1; s >= 0; --s) {
+    for (size_t k = 0; k < 3 * n; ++k) ab[k] = h * vb[k] + carry[k];
+    direct_vjp(xs.data() + 3 * n * (size_t)(s + 1), mass, n, e2, ab.data(), nthreads, xb.data(), mb.data());
+    for (size_t k = 0; k < 3 * n; ++k) {
+      vb[k] += dt * xb[k];
+      carry[k] = h * vb[k];
+    }
+  }
+  direct_vjp(xs.data(), mass, n, e2, carry.data(), nthreads, xb.data(), mb.data());
+  std::memcpy(gx, xb.data(), 3 * n * sizeof(double));
+  std::memcpy(gv, vb.data(), 3 * n * sizeof(double));
+  std::memcpy(gm, mb.data(), n * sizeof(double));
 }
 
 }  // extern "C"

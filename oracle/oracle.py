@@ -51,6 +51,13 @@ class Restatement:
         lib.orc_kick.argtypes = [P, P, S, D]
         lib.orc_steps.argtypes = [P, P, P, P, S, D, D, D, D, I, I, I, I, I, P, P]
         lib.orc_time_sample.argtypes = [P, P, S, P, D, I, I, D, D, P, S, I, P, P, P]
+        lib.orc_frozen_record.argtypes = [P, P, P, S, D, D, D, D, I, I, I, P, P]
+        lib.orc_frozen_record.restype = P
+        lib.orc_frozen_run.argtypes = [P, P, P, P, I, P, P]
+        lib.orc_frozen_entries.argtypes = [P]
+        lib.orc_frozen_entries.restype = L
+        lib.orc_frozen_free.argtypes = [P]
+        lib.orc_direct_adjoint.argtypes = [P, P, P, S, D, D, I, P, P, I, P, P, P, P, P]
         self.lib = lib
 
     def bounds(self, pos):
@@ -148,6 +155,53 @@ class Restatement:
         self.lib.orc_time_sample(_p(pos), _p(mass), len(pos), _p(c), edge, leaf_capacity, mode, theta, eps, _p(t),
                                  len(t), nthreads, _p(b), _p(w), _p(acc))
         return float(b[0]), float(w[0]), acc
+
+
+class FrozenTrajectory:
+    """FP64 KDK trajectory of the library's differentiable path with the interaction lists of
+    its own forward pass held fixed; run() re-evaluates that map from another initial state
+    (the function whose finite differences the adjoint must match)."""
+
+    def __init__(self, orc, pos, vel, mass, dt, theta, eps, edge_factor, leaf_capacity, nsteps, nthreads=8):
+        self.lib = orc.lib
+        self.n = len(pos)
+        self.nthreads = nthreads
+        pos, vel, mass = _f64(pos, 3), _f64(vel, 3), _f64(mass)
+        self.final_pos = np.zeros_like(pos)
+        self.final_vel = np.zeros_like(vel)
+        self.h = self.lib.orc_frozen_record(_p(pos), _p(vel), _p(mass), self.n, dt, theta, eps, edge_factor,
+                                            leaf_capacity, nsteps, nthreads, _p(self.final_pos), _p(self.final_vel))
+
+    def entries(self):
+        return self.lib.orc_frozen_entries(self.h)
+
+    def run(self, pos, vel, mass):
+        pos, vel, mass = _f64(pos, 3), _f64(vel, 3), _f64(mass)
+        xo = np.zeros_like(pos)
+        vo = np.zeros_like(vel)
+        self.lib.orc_frozen_run(self.h, _p(pos), _p(vel), _p(mass), self.nthreads, _p(xo), _p(vo))
+        return xo, vo
+
+    def close(self):
+        if self.h:
+            self.lib.orc_frozen_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def direct_adjoint(orc, pos, vel, mass, dt, eps, nsteps, dl_dx, dl_dv=None, nthreads=8):
+    """FP64 direct-sum KDK trajectory and its adjoint: (final pos, final vel, d pos0, d vel0, d mass)."""
+    pos, vel, mass = _f64(pos, 3), _f64(vel, 3), _f64(mass)
+    n = len(pos)
+    gx = None if dl_dx is None else _f64(dl_dx, 3)
+    gvin = None if dl_dv is None else _f64(dl_dv, 3)
+    xo, vo = np.zeros((n, 3)), np.zeros((n, 3))
+    gx0, gv0, gm = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n)
+    orc.lib.orc_direct_adjoint(_p(pos), _p(vel), _p(mass), n, dt, eps, nsteps, _p(gx), _p(gvin), nthreads, _p(xo),
+                               _p(vo), _p(gx0), _p(gv0), _p(gm))
+    return xo, vo, gx0, gv0, gm
 
 
 class RefLiteral:

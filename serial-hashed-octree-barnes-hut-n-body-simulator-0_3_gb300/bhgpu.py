@@ -28,7 +28,7 @@ BH_MULTIPOLE_QUADRUPOLE = 1
 STATUS = {
     0: "BH_OK", 1: "BH_ERR_INVALID_ARG", 2: "BH_ERR_OOM", 3: "BH_ERR_DEVICE", 4: "BH_ERR_OVERFLOW_STACK",
     5: "BH_ERR_OVERFLOW_HASH", 6: "BH_ERR_OVERFLOW_NODES", 7: "BH_ERR_TIMEOUT", 8: "BH_ERR_NO_TREE",
-    9: "BH_ERR_NOT_FOUND",
+    9: "BH_ERR_NOT_FOUND", 10: "BH_ERR_OVERFLOW_TAPE",
 }
 
 EXPORTS = [
@@ -37,7 +37,8 @@ EXPORTS = [
     "bh_sort_bodies", "bh_build", "bh_tree_size", "bh_tree_nodes", "bh_node_lookup", "bh_force",
     "bh_kick_drift", "bh_kick", "bh_step", "bh_params_default", "bh_synchronize", "bh_event_record",
     "bh_event_elapsed_ms", "bh_flush_l2", "bh_host_alloc", "bh_host_free", "bh_measure_fp32_peak",
-    "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step",
+    "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step", "bh_adjoint_forward",
+    "bh_step_backward",
 ]
 
 
@@ -122,6 +123,8 @@ def load():
         "bh_sort_keys_static": ([P, P, P, P, S, P, P], I),
         "bh_batch_set": ([P, P, P, P, S], I),
         "bh_batch_step": ([P, ctypes.POINTER(Params), I, ctypes.POINTER(Stats)], I),
+        "bh_adjoint_forward": ([P, ctypes.POINTER(Params), I, I, ctypes.POINTER(Stats)], I),
+        "bh_step_backward": ([P, P, P, P, P, P, ctypes.POINTER(Stats)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -291,6 +294,32 @@ class Simulation:
         check(self.lib.bh_batch_step(self.h, ctypes.byref(params), nsteps, ctypes.byref(st) if stats else None),
               "bh_batch_step")
         return st
+
+    def adjoint_forward(self, params, nsteps, checkpoint_every, stats=True):
+        """Differentiable trajectory: nsteps KDK steps in upload order with checkpoints."""
+        st = Stats()
+        check(self.lib.bh_adjoint_forward(self.h, ctypes.byref(params), nsteps, checkpoint_every,
+                                          ctypes.byref(st) if stats else None), "bh_adjoint_forward")
+        return st
+
+    def step_backward(self, dl_dpos, dl_dvel, stats=False):
+        """Gradients (d pos0 (n, 4), d vel0 (n, 4), d mass (n,)) of a loss whose gradients with
+        respect to the final positions / velocities are dl_dpos / dl_dvel ((n, 3) or (n, 4), or None)."""
+        def as4(a):
+            if a is None:
+                return None
+            a = np.asarray(a, np.float32)
+            out = np.zeros((self.n, 4), np.float32)
+            out[:, :3] = a[:, :3]
+            return out
+        gx = np.zeros((self.n, 4), np.float32)
+        gv = np.zeros((self.n, 4), np.float32)
+        gm = np.zeros(self.n, np.float32)
+        st = Stats()
+        bx, bv = as4(dl_dpos), as4(dl_dvel)  # kept alive across the call
+        check(self.lib.bh_step_backward(self.h, _ptr(bx), _ptr(bv), _ptr(gx), _ptr(gv), _ptr(gm), ctypes.byref(st)),
+              "bh_step_backward")
+        return (gx, gv, gm, st) if stats else (gx, gv, gm)
 
     def synchronize(self):
         check(self.lib.bh_synchronize(self.h), "bh_synchronize")

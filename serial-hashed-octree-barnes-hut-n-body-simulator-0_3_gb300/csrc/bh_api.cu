@@ -13,33 +13,8 @@
 
 using bh::kLevels;
 
-namespace {
-
-constexpr size_t kMaxBodies = (1u << 30) - 1;  // sort look-back words hold 30-bit counts
-
-template <class T>
-bh_status dalloc(T** p, size_t count) {
-  *p = nullptr;
-  if (count == 0) count = 1;
-  if (cudaMalloc((void**)p, sizeof(T) * count) != cudaSuccess) {
-    cudaGetLastError();
-    *p = nullptr;
-    return BH_ERR_OOM;
-  }
-  return BH_OK;
-}
-
-template <class T>
-void dfree(T*& p) {
-  if (p) cudaFree((void*)p);
-  p = nullptr;
-}
-
-#define BH_TRY(expr)                     \
-  do {                                   \
-    bh_status s_ = (expr);               \
-    if (s_ != BH_OK) return s_;          \
-  } while (0)
+// Host helpers shared with the other translation units (declared in bh_internal.cuh).
+namespace bh {
 
 bh_status cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return BH_OK;
@@ -102,7 +77,7 @@ bh_status ensure_hash(bh_ctx* c) {
 }
 
 // Reads the device error word (and the counters) after finishing the stream.
-bh_status sync_and_check(bh_ctx* c, uint32_t* err_out = nullptr) {
+bh_status sync_and_check(bh_ctx* c, uint32_t* err_out) {
   cudaMemcpyAsync(c->h_err, c->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
   cudaMemcpyAsync(c->h_counters, c->counters, sizeof(bh::Counters), cudaMemcpyDeviceToHost, c->stream);
   cudaMemcpyAsync(c->h_level_bounds, c->level_bounds, sizeof(int) * (kLevels + 2), cudaMemcpyDeviceToHost,
@@ -139,6 +114,12 @@ float elapsed(bh_ctx* c, int a, int b) {
   return ms;
 }
 
+}  // namespace bh
+
+using namespace bh;
+
+namespace {
+constexpr size_t kMaxBodies = (1u << 30) - 1;  // sort look-back words hold 30-bit counts
 }  // namespace
 
 extern "C" {
@@ -204,6 +185,7 @@ bh_status bh_destroy(bh_ctx* c) {
   dfree(c->hash_vals);
   for (auto& g : c->graph)
     if (g) cudaGraphExecDestroy(g);
+  bh::adj_release(c);
   dfree(c->sys_off);
   dfree(c->sys_geom);
   dfree(c->body_sys);
@@ -297,6 +279,7 @@ bh_status bh_set_state(bh_ctx* c, const float* pos_m4, const float* vel4, const 
   c->cur = 0;
   c->tree_valid = false;
   c->batch = false;
+  bh::adj_invalidate(c);
   for (auto& g : c->graph)
     if (g) {
       cudaGraphExecDestroy(g);

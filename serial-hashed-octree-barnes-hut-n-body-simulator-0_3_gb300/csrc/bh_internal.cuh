@@ -17,6 +17,7 @@ enum : uint32_t {
   kErrHash = 1u << (BH_ERR_OVERFLOW_HASH - 3),
   kErrNodes = 1u << (BH_ERR_OVERFLOW_NODES - 3),
   kErrTimeout = 1u << (BH_ERR_TIMEOUT - 3),
+  kErrTape = 1u << (BH_ERR_OVERFLOW_TAPE - 3),
 };
 
 // Geometry of one step, produced on the device by the bounds kernel (or set by the host
@@ -56,6 +57,16 @@ struct __align__(16) NodeUp {
   float q[6];         // Qxx, Qxy, Qxz, Qyy, Qyz, Qzz about the centre of mass
   uint32_t min_rank;  // smallest Morton slot among members (literal barycentre)
   uint32_t pad;
+};
+
+// One recorded evaluation buffer of the walk (the adjoint replays these): the group it served
+// (first body in tree order, body count), the kind (0 cells, 1 points), the entry count, and
+// per entry the node (cells) or point index (>= 0 body in tree order, < 0 -(node + 1)) and the
+// 32-bit mask of lanes that took it.
+struct __align__(16) Chunk {
+  int4 hdr;
+  int idx[32];
+  uint32_t mask[32];
 };
 
 struct Counters {
@@ -152,9 +163,45 @@ struct bh_ctx {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // captured batched step, by state parity
   bh_params graph_params = {};
   uint64_t launches = 0;  // kernels launched on this context (every launcher adds its count)
+
+  void* adj = nullptr;  // differentiable-path state (checkpoints, tape, adjoints): bh_adjoint.cu
 };
 
 namespace bh {
+
+// ---- host helpers (bh_api.cu) ----
+template <class T>
+inline bh_status dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  if (cudaMalloc((void**)p, sizeof(T) * count) != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return BH_ERR_OOM;
+  }
+  return BH_OK;
+}
+
+template <class T>
+inline void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+#define BH_TRY(expr)            \
+  do {                          \
+    bh_status s_ = (expr);      \
+    if (s_ != BH_OK) return s_; \
+  } while (0)
+
+bh_status cuda_status(cudaError_t e);
+bh_status last_launch();
+bh_status err_to_status(uint32_t e);
+bh_status ensure_nodes(bh_ctx* c, size_t need);
+// Reads the device error word, the counters and the level bounds after finishing the stream.
+bh_status sync_and_check(bh_ctx* c, uint32_t* err_out = nullptr);
+void clear_device_flags(bh_ctx* c);
+float elapsed(bh_ctx* c, int a, int b);
 
 // Kernel launchers (defined in the .cu files; all asynchronous on `st`).
 // Stable LSD radix sort by 8-bit digits first_pass .. first_pass + npasses - 1 of the keys
@@ -187,6 +234,12 @@ void launch_hash(bh_ctx* c);
 void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc_slot, float4* vel_kick,
                  float half_dt, bool batch = false);
 void launch_lookup(bh_ctx* c, uint64_t key, int* out_index);
+void launch_walk_record(bh_ctx* c, int n, float theta, float eps, float4* acc_slot, float4* vel_kick, float half_dt,
+                        Chunk* tape, unsigned* tape_count, int tape_cap);
 void launch_fp32_peak(cudaStream_t st, float* sink, int blocks);
+// Frees the differentiable-path state of the context.
+void adj_release(bh_ctx* c);
+// Marks the recorded trajectory stale (new bodies were uploaded).
+void adj_invalidate(bh_ctx* c);
 
 }  // namespace bh

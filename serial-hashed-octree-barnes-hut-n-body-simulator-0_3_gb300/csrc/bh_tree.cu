@@ -246,7 +246,7 @@ __global__ __launch_bounds__(kThreads) void k_gather_kd_treekey(
     uint64_t* __restrict__ tkeys, uint32_t* __restrict__ tidx) {
   int j = blockIdx.x * kThreads + threadIdx.x;
   if (j >= n) return;
-  uint32_t i = perm[j];
+  const uint32_t i = perm ? perm[j] : (uint32_t)j;  // no permutation: bodies keep their order
   float4 p = pin[i], v = vin[i], a = acc[acc_follows_body ? i : (uint32_t)j];
   v.x += a.x * half_dt;
   v.y += a.y * half_dt;

@@ -73,13 +73,42 @@ struct Acc {
   }
 };
 
+// Interaction recording for the adjoint: where the flushed buffers go, and the current group.
+struct Rec {
+  Chunk* chunks;
+  unsigned* count;
+  int cap;
+  int gbase, gcount;
+  uint32_t* err;
+};
+
+// Appends one flushed buffer (cnt entries of idx / mask, still in shared memory) to the tape.
+__device__ __forceinline__ void record_chunk(const Rec& r, int kind, int cnt, const int* idx, const uint32_t* mask,
+                                             int lane) {
+  unsigned slot = 0;
+  if (lane == 0) slot = atomicAdd(r.count, 1u);
+  slot = __shfl_sync(0xffffffffu, slot, 0);
+  if (slot >= (unsigned)r.cap) {
+    if (lane == 0) atomicOr(r.err, kErrTape);
+    return;
+  }
+  Chunk& ch = r.chunks[slot];
+  if (lane == 0) ch.hdr = make_int4(r.gbase, r.gcount, kind, cnt);
+  if (lane < cnt) {
+    ch.idx[lane] = idx[lane];
+    ch.mask[lane] = mask[lane];
+  }
+}
+
 // 32 multipole cells (monopole + quadrupole). The lane mask rides in st2.w.
+template <bool kRec>
 __device__ __forceinline__ void eval_cells(WarpSmem& s, int cnt, const WalkNode* __restrict__ nodes,
                                            uint32_t lanebit, float px, float py, float pz, float eps2, Acc& acc,
-                                           unsigned long long& ev) {
+                                           unsigned long long& ev, const Rec& rec) {
   ev += (unsigned)cnt;
   __syncwarp();
   const int lane = __ffs(lanebit) - 1;
+  if (kRec) record_chunk(rec, 0, cnt, s.cell_node, s.cell_mask, lane);
   if (lane < cnt) {
     const WalkNode* nd = nodes + s.cell_node[lane];
     s.st0[lane] = __ldg(&nd->mac);
@@ -119,13 +148,14 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cnt, const WalkNode*
 }
 
 // Up to 32 point masses. The lane mask is read from pt_mask.
-template <bool kSelfTest>
+template <bool kSelfTest, bool kRec>
 __device__ __forceinline__ void eval_points(WarpSmem& s, int cnt, const WalkNode* __restrict__ nodes,
                                             const float4* __restrict__ tpos, uint32_t lanebit, float px, float py,
-                                            float pz, float eps2, Acc& acc, unsigned long long& ev) {
+                                            float pz, float eps2, Acc& acc, unsigned long long& ev, const Rec& rec) {
   ev += (unsigned)cnt;
   __syncwarp();
   const int lane = __ffs(lanebit) - 1;
+  if (kRec) record_chunk(rec, 1, cnt, s.pt_idx, s.pt_mask, lane);
   if (lane < cnt) {
     const int e = s.pt_idx[lane];
     float4 v;
@@ -176,14 +206,16 @@ __device__ __forceinline__ void shift_down(int* idx, uint32_t* msk, int n, int l
   }
 }
 
-template <bool kQuad, bool kSelfTest>
+template <bool kQuad, bool kSelfTest, bool kRec = false>
 __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ nodes,
                                                    const float4* __restrict__ tpos,
                                                    const uint32_t* __restrict__ tslot, int n, float theta2,
                                                    float eps2, float4* __restrict__ acc_slot,
                                                    float4* __restrict__ vel_kick, float half_dt,
                                                    const int4* __restrict__ groups, int ngroups_table,
-                                                   Counters* __restrict__ ctr, uint32_t* __restrict__ err) {
+                                                   Counters* __restrict__ ctr, uint32_t* __restrict__ err,
+                                                   Chunk* __restrict__ tape = nullptr,
+                                                   unsigned* __restrict__ tape_count = nullptr, int tape_cap = 0) {
   __shared__ WarpSmem smem[kWarps];
   const int lane = threadIdx.x & 31;
   const uint32_t lanebit = 1u << lane;
@@ -216,6 +248,7 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
       root = 0;
     }
     const int4 root_link = __ldg(&nodes[root].link);
+    const Rec rec{tape, tape_count, tape_cap, gbase, gcount, err};
     const int i = gbase + lane;
     const bool valid = lane < gcount;
     const float4 p = __ldg(tpos + (valid ? i : gbase));
@@ -247,7 +280,7 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
           s.pt_mask[lane] = active;
         }
         if (lane == 0) cnt_pt += (long long)k * __popc(active);
-        eval_points<kSelfTest>(s, k, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt);
+        eval_points<kSelfTest, kRec>(s,k, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt, rec);
       }
       if (lane == 0) cnt_pt -= __popc(active);
     } else {
@@ -354,7 +387,7 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
           }
           ncell += __popc(bal);
           if (ncell >= 32) {
-            eval_cells(s, 32, nodes, lanebit, p.x, p.y, p.z, eps2, acc, ev_cell);
+            eval_cells<kRec>(s,32, nodes, lanebit, p.x, p.y, p.z, eps2, acc, ev_cell, rec);
             shift_down(s.cell_node, s.cell_mask, ncell, lane);
             ncell -= 32;
           }
@@ -372,7 +405,7 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
           }
           npt += __popc(bal);
           if (npt >= 32) {
-            eval_points<kSelfTest>(s, 32, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt);
+            eval_points<kSelfTest, kRec>(s,32, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt, rec);
             shift_down(s.pt_idx, s.pt_mask, npt, lane);
             npt -= 32;
           }
@@ -437,7 +470,7 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
             }
             npt += kk;
             if (npt >= 32) {
-              eval_points<kSelfTest>(s, 32, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt);
+              eval_points<kSelfTest, kRec>(s,32, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt, rec);
               shift_down(s.pt_idx, s.pt_mask, npt, lane);
               npt -= 32;
             }
@@ -446,8 +479,8 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
         }
       }
     }
-    if (ncell > 0) eval_cells(s, ncell, nodes, lanebit, p.x, p.y, p.z, eps2, acc, ev_cell);
-    if (npt > 0) eval_points<kSelfTest>(s, npt, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt);
+    if (ncell > 0) eval_cells<kRec>(s,ncell, nodes, lanebit, p.x, p.y, p.z, eps2, acc, ev_cell, rec);
+    if (npt > 0) eval_points<kSelfTest, kRec>(s,npt, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt, rec);
     if (valid) {
       const uint32_t slot = __ldg(tslot + i);
       const float ax = acc.sx, ay = acc.sy, az = acc.sz;
@@ -534,6 +567,24 @@ void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc
     else
       launch_walk_t<false, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
   }
+}
+
+}  // namespace bh
+
+namespace bh {
+
+// The walk of the differentiable path: quadrupole multipoles, positive softening, and every
+// flushed interaction buffer appended to `tape` (tape_count counts chunks; overflow of tape_cap
+// sets the tape error bit).
+void launch_walk_record(bh_ctx* c, int n, float theta, float eps, float4* acc_slot, float4* vel_kick, float half_dt,
+                        Chunk* tape, unsigned* tape_count, int tape_cap) {
+  if (n <= 0) return;
+  cudaMemsetAsync(&c->counters->group_next, 0, sizeof(unsigned), c->stream);
+  c->launches += 1;
+  const int grid = min(walk_grid<true, false>(), ((n + 31) / 32) / kWarps + 1);
+  k_walk<true, false, true><<<grid, kThreads, 0, c->stream>>>(c->wnode, c->tpos, c->tslot, n, theta * theta,
+                                                              eps * eps, acc_slot, vel_kick, half_dt, nullptr, 0,
+                                                              c->counters, c->err, tape, tape_count, tape_cap);
 }
 
 }  // namespace bh
