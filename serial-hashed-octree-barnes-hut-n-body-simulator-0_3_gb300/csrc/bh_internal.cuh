@@ -30,6 +30,11 @@ struct Geom {
   double tedge;      // tree root edge
   double tscale;     // 2^21 / tedge
   double tmargin;    // fast-path margin in key units (see tree_key)
+  // float-float splits (value = hi + lo) of the fields above for the FP32 fast paths of the
+  // key kernels (GB300's FP64 pipe is far slower than its FP32 pipe)
+  float size_hi, size_lo, frac_hi, frac_lo;
+  float tc_hi[3], tc_lo[3];
+  float tscale_hi, tscale_lo, tmargin_f;
 };
 
 // Walk record of one node: 64 bytes, read by the tree walk.

@@ -20,7 +20,13 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 16;
+#ifndef BH_SORT_ITEMS
+#define BH_SORT_ITEMS 16
+#endif
+#ifndef BH_SORT_MIN_BLOCKS
+#define BH_SORT_MIN_BLOCKS 2
+#endif
+constexpr int kItems = BH_SORT_ITEMS;     // keys per thread
 constexpr int kTile = kThreads * kItems;  // 4096 keys
 constexpr int kPasses = 8;
 constexpr int kRadix = 256;
@@ -28,6 +34,7 @@ constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValMask = (1u << 30) - 1;
 constexpr int kSpinLimit = 1 << 22;  // about a second of polling; then the sort reports a timeout
+constexpr int kLookWindow = 8;       // predecessor tiles read per look-back round trip
 
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
   uint32_t v;
@@ -108,7 +115,8 @@ struct OnesweepSmem {
   uint32_t tile;
 };
 
-__global__ __launch_bounds__(kThreads) void k_onesweep(const uint64_t* __restrict__ kin,
+// Two resident blocks per SM (the shared-memory tile allows three; registers cap it at two).
+__global__ __launch_bounds__(kThreads, BH_SORT_MIN_BLOCKS) void k_onesweep(const uint64_t* __restrict__ kin,
                                                        const uint32_t* __restrict__ vin,
                                                        uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                        int n, int shift, const uint32_t* __restrict__ digit_off,
@@ -142,8 +150,15 @@ __global__ __launch_bounds__(kThreads) void k_onesweep(const uint64_t* __restric
     long long idx = wbase + j * 32 + lane;
     bool ok = idx < n;
     uint32_t d = (uint32_t)(key[j] >> shift) & 0xFFu;
-    uint32_t tag = ok ? d : (0x100u + (uint32_t)lane);  // invalid lanes never match
-    uint32_t peers = __match_any_sync(0xffffffffu, tag);
+    // lanes holding the same digit: one ballot per digit bit (a multisplit by ballots, which
+    // issues faster than the match instruction); invalid lanes are nobody's peers
+    uint32_t peers = __ballot_sync(0xffffffffu, ok);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const bool bit = (d >> b) & 1u;
+      const uint32_t vote = __ballot_sync(0xffffffffu, bit);
+      peers &= bit ? vote : ~vote;
+    }
     uint32_t pre = ok ? s.warp_cnt[w][d] : 0u;
     __syncwarp();
     if (ok && lane == __ffs(peers) - 1) s.warp_cnt[w][d] = pre + __popc(peers);
@@ -190,25 +205,37 @@ __global__ __launch_bounds__(kThreads) void k_onesweep(const uint64_t* __restric
     }
   }
 
-  // decoupled look-back for digit t
+  // decoupled look-back for digit t, reading a window of kLookWindow predecessors per round
+  // trip (independent loads in flight together) instead of one tile at a time
   uint32_t excl = 0;
   if (tile > 0) {
     long long k = (long long)tile - 1;
     int spins = 0;
     while (k >= 0) {
-      uint32_t v = ld_relaxed(lookback + (size_t)k * kRadix + t);
-      uint32_t flag = v & ~kValMask;
-      if (flag == 0) {
+      uint32_t v[kLookWindow];
+#pragma unroll
+      for (int q = 0; q < kLookWindow; ++q)  // tile 0 always holds a prefix, so k - q < 0 is never consumed
+        v[q] = (k - q >= 0) ? ld_relaxed(lookback + (size_t)(k - q) * kRadix + t) : kFlagPrefix;
+      int used = 0;
+      bool done = false;
+#pragma unroll
+      for (int q = 0; q < kLookWindow; ++q) {
+        if (done || used < q) continue;  // stop at a prefix or at the first tile not yet published
+        const uint32_t flag = v[q] & ~kValMask;
+        if (flag == 0) continue;
+        excl += v[q] & kValMask;
+        used = q + 1;
+        done = flag == kFlagPrefix;
+      }
+      if (done) break;
+      k -= used;
+      if (used == 0) {
         if (++spins > kSpinLimit) {
           atomicOr(err, kErrTimeout);
           break;
         }
         __nanosleep(32);
-        continue;
       }
-      excl += v & kValMask;
-      if (flag == kFlagPrefix) break;
-      --k;
     }
     st_relaxed(my_lb, kFlagPrefix | ((excl + total) & kValMask));
   }

@@ -27,6 +27,54 @@ __device__ __forceinline__ uint64_t spread_bits(uint64_t v) {
   return v;
 }
 
+// Float-float arithmetic (a value is hi + lo): TwoSum (Knuth), FMA-based TwoProduct and a
+// Newton-corrected quotient (Dekker 1971). About 44 significant bits from FP32 operations.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_norm(float s, float e) {
+  const float hi = s + e;
+  return {hi, e - (hi - s)};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  float e = (a.hi - (s - bb)) + (b.hi - bb);
+  e += a.lo + b.lo;
+  return ff_norm(s, e);
+}
+__device__ __forceinline__ FF ff_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return ff_norm(p, e);
+}
+__device__ __forceinline__ FF ff_div(FF n, FF d) {
+  const float q = n.hi / d.hi;
+  const float p = q * d.hi;
+  const float pe = fmaf(q, d.hi, -p);
+  const float r = (((n.hi - p) - pe) + fmaf(-q, d.lo, n.lo)) / d.hi;
+  return ff_norm(q, r);
+}
+// Splits a double into a float-float pair (hi = nearest float, lo = nearest float of the rest):
+// the pair matches the double to about 2^-48 relative.
+__device__ __forceinline__ void ff_split(double x, float& hi, float& lo) {
+  hi = __double2float_rn(x);
+  lo = __double2float_rn(__dsub_rn(x, (double)hi));
+}
+
+// x ~ n + f from a float-float value: n = nearest integer of hi (exactly representable), f the
+// signed remainder (|f| <= 0.5 + |lo|), accurate to the pair's own error.
+__device__ __forceinline__ void ff_int_frac(FF x, float& n, float& f) {
+  n = rintf(x.hi);
+  f = (x.hi - n) + x.lo;
+}
+
 // The reference's (spatialKey)(double) cast (src/MortonKeys.hpp:162-164) as x86-64 code
 // generated by gcc evaluates it: below 2^63 (or NaN) a signed truncation, 0x8000000000000000
 // when that is out of range; otherwise a truncation of x - 2^63 with bit 63 flipped.
@@ -40,12 +88,35 @@ __device__ __forceinline__ uint64_t x86_trunc_u64(double x) {
   return 0ull;
 }
 
-// computeMortonKey (src/MortonKeys.hpp:137-181): (p + S) * frac per axis, converted, then
-// interleaved x<<2 | y<<1 | z with bit 63 set (interleaveBits, :95-124).
-__device__ __forceinline__ uint64_t morton_key(float4 p, double S, double frac) {
-  uint64_t wx = x86_trunc_u64(__dmul_rn(__dadd_rn((double)p.x, S), frac));
-  uint64_t wy = x86_trunc_u64(__dmul_rn(__dadd_rn((double)p.y, S), frac));
-  uint64_t wz = x86_trunc_u64(__dmul_rn(__dadd_rn((double)p.z, S), frac));
+// One axis of computeMortonKey (src/MortonKeys.hpp:137-181) in the reference's own FP64
+// arithmetic: (p + S) * frac, then the cast.
+__device__ __noinline__ uint64_t morton_coord_exact(float x, double S, double frac) {
+  return x86_trunc_u64(__dmul_rn(__dadd_rn((double)x, S), frac));
+}
+
+// The same axis with an FP32 fast path. v = (p + S) * frac is formed in float-float: for
+// |v| < 2^22 the pair is within 2^-23 of the exact v, and the reference's two FP64 roundings put
+// its value within |v| 2^-52 <= 2^-30 of it. When the pair lies farther than 2^-21 from every
+// integer, both therefore truncate to the same integer, which the fast path returns (as the
+// 64-bit two's-complement word the cast produces for |v| < 2^63). Otherwise (near an integer,
+// |v| >= 2^22, or not finite) the FP64 path decides.
+__device__ __forceinline__ uint64_t morton_coord(float x, const Geom& g) {
+  const FF v = ff_mul(ff_add({x, 0.f}, {g.size_hi, g.size_lo}), {g.frac_hi, g.frac_lo});
+  float n, f;
+  ff_int_frac(v, n, f);
+  if (fabsf(v.hi) < 0x1p22f && fabsf(f) > 0x1p-21f) {
+    const bool pos = n > 0.f || (n == 0.f && f > 0.f);
+    // truncation toward zero: floor for positive v, ceiling for negative v
+    const float q = pos ? (f < 0.f ? n - 1.f : n) : (f > 0.f ? n + 1.f : n);
+    return (uint64_t)(long long)q;
+  }
+  return morton_coord_exact(x, g.size, g.frac);
+}
+
+// computeMortonKey: the three axes interleaved x<<2 | y<<1 | z with bit 63 set
+// (interleaveBits, src/MortonKeys.hpp:95-124).
+__device__ __forceinline__ uint64_t morton_key(float4 p, const Geom& g) {
+  const uint64_t wx = morton_coord(p.x, g), wy = morton_coord(p.y, g), wz = morton_coord(p.z, g);
   return (1ull << 63) | (spread_bits(wx) << 2) | (spread_bits(wy) << 1) | spread_bits(wz);
 }
 
@@ -68,29 +139,34 @@ __device__ __noinline__ uint32_t tree_path_exact(double p, double c0, double E) 
 // Same path from one scaled coordinate. In exact arithmetic the level-d comparison points
 // are the integers of [1, 2^21 - 1] in the units u = (p - c0) * 2^21 / E + 2^20, and the
 // strict '>' makes the path ceil(u) - 1 clamped to [0, 2^21 - 1]. The reference's rounded
-// centres differ from the exact ones by at most 21 half-ulps, and u carries a few ulps of its
-// own; together that is below 2^-26 * (1 + |c0| / E) key units. Whenever u lies closer than
-// the margin (2^-20 * (1 + |c0| / E)) to a comparison point, or is not finite, the exact
-// recurrence decides instead.
-__device__ __forceinline__ uint32_t tree_path(double p, double c0, double E, double scale, double margin) {
-  double u = __dadd_rn(__dmul_rn(__dsub_rn(p, c0), scale), 1048576.0);
-  double dist;
-  if (u < 1.0)
-    dist = 1.0 - u;
-  else if (u > 2097151.0)
-    dist = u - 2097151.0;
-  else
-    dist = fabs(u - rint(u));
-  if (!(dist > margin)) return tree_path_exact(p, c0, E);
-  double cu = ceil(u) - 1.0;
-  cu = fmin(fmax(cu, 0.0), 2097151.0);
-  return (uint32_t)cu;
+// centres differ from the exact ones by at most 21 half-ulps: below 2^-26 * (1 + |c0| / E) key
+// units. u is formed in float-float (the splits of c0 and 2^21 / E and the pair arithmetic add
+// below 2^-24 * (1 + |c0| / E)). Whenever u lies closer than the margin
+// (2^-20 * (1 + |c0| / E)) to a comparison point, or is not finite, the exact recurrence
+// decides instead.
+__device__ __forceinline__ uint32_t tree_path(float p, int a, const Geom& g) {
+  const FF d = ff_add({p, 0.f}, {-g.tc_hi[a], -g.tc_lo[a]});
+  const FF u = ff_add(ff_mul(d, {g.tscale_hi, g.tscale_lo}), {1048576.f, 0.f});
+  float n, f;
+  ff_int_frac(u, n, f);
+  float dist;
+  uint32_t path;
+  if (n < 1.f || (n == 1.f && f < 0.f)) {  // u < 1
+    dist = (1.f - n) - f;
+    path = 0u;
+  } else if (n > 2097151.f || (n == 2097151.f && f > 0.f)) {  // u > 2^21 - 1
+    dist = (n - 2097151.f) + f;
+    path = 2097151u;
+  } else {
+    dist = fabsf(f);
+    path = (uint32_t)(f < 0.f ? n - 1.f : n);
+  }
+  if (dist > g.tmargin_f) return path;  // false for NaN
+  return tree_path_exact((double)p, g.tc[a], g.tedge);
 }
 
 __device__ __forceinline__ uint64_t tree_key(float4 p, const Geom& g) {
-  uint32_t kx = tree_path((double)p.x, g.tc[0], g.tedge, g.tscale, g.tmargin);
-  uint32_t ky = tree_path((double)p.y, g.tc[1], g.tedge, g.tscale, g.tmargin);
-  uint32_t kz = tree_path((double)p.z, g.tc[2], g.tedge, g.tscale, g.tmargin);
+  const uint32_t kx = tree_path(p.x, 0, g), ky = tree_path(p.y, 1, g), kz = tree_path(p.z, 2, g);
   return (1ull << 63) | (spread_bits(kx) << 2) | (spread_bits(ky) << 1) | spread_bits(kz);
 }
 
@@ -102,6 +178,12 @@ __device__ __forceinline__ void fill_tree_geom(Geom& g, const double tc[3], doub
   g.tscale = __ddiv_rn(2097152.0, tedge);
   double cm = fmax(fabs(tc[0]), fmax(fabs(tc[1]), fabs(tc[2])));
   g.tmargin = 0x1p-20 * (1.0 + cm / tedge);
+  // float-float copies for the key fast paths (size and frac are set by every caller first)
+  ff_split(g.size, g.size_hi, g.size_lo);
+  ff_split(g.frac, g.frac_hi, g.frac_lo);
+  for (int a = 0; a < 3; ++a) ff_split(tc[a], g.tc_hi[a], g.tc_lo[a]);
+  ff_split(g.tscale, g.tscale_hi, g.tscale_lo);
+  g.tmargin_f = __double2float_rn(g.tmargin);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -213,7 +295,7 @@ __global__ __launch_bounds__(kThreads) void k_morton(const float4* __restrict__ 
   int i = blockIdx.x * kThreads + threadIdx.x;
   if (i >= n) return;
   const Geom& gg = body_sys ? g[body_sys[i]] : *g;
-  keys[i] = morton_key(pos[i], gg.size, gg.frac);
+  keys[i] = morton_key(pos[i], gg);
   idx[i] = (uint32_t)i;
 }
 
@@ -455,41 +537,6 @@ __global__ __launch_bounds__(kThreads) void k_level(int d, const uint64_t* __res
 // ---------------------------------------------------------------------------------------
 // upsweep
 // ---------------------------------------------------------------------------------------
-
-// Float-float arithmetic (a value is hi + lo): TwoSum (Knuth), FMA-based TwoProduct and a
-// Newton-corrected quotient (Dekker 1971). About 44 significant bits from FP32 operations.
-struct FF {
-  float hi, lo;
-};
-__device__ __forceinline__ FF ff_norm(float s, float e) {
-  const float hi = s + e;
-  return {hi, e - (hi - s)};
-}
-__device__ __forceinline__ FF ff_add(FF a, FF b) {
-  const float s = a.hi + b.hi;
-  const float bb = s - a.hi;
-  float e = (a.hi - (s - bb)) + (b.hi - bb);
-  e += a.lo + b.lo;
-  return ff_norm(s, e);
-}
-__device__ __forceinline__ FF ff_prod(float a, float b) {
-  const float p = a * b;
-  return {p, fmaf(a, b, -p)};
-}
-__device__ __forceinline__ FF ff_mul(FF a, FF b) {
-  const float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  return ff_norm(p, e);
-}
-__device__ __forceinline__ FF ff_div(FF n, FF d) {
-  const float q = n.hi / d.hi;
-  const float p = q * d.hi;
-  const float pe = fmaf(q, d.hi, -p);
-  const float r = (((n.hi - p) - pe) + fmaf(-q, d.lo, n.lo)) / d.hi;
-  return ff_norm(q, r);
-}
 
 // Parallel-axis quadrupole contribution of one child (or member body) of mass m at offset x
 // from the node's centre of mass, the reference's formulas (src/HashedOctree.cpp:778-808).

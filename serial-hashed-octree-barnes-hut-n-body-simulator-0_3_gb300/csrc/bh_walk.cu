@@ -135,7 +135,8 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cnt, const WalkNode*
     const float qr = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
     // a += d (m / D^3 + 2.5 (d.Q.d) / D^7) - Q.d / D^5
     const float radial = fmaf(qr, w5 * (2.5f * u), c1.x * w3);
-    // selects rather than a branch: every lane runs the same straight-line code
+    // selects rather than a branch: every lane runs the same straight-line code (a select on
+    // 1/D instead, zeroing every term, puts the select on the dependent chain and runs slower)
     const bool take = (__float_as_uint(c2.w) & lanebit) != 0u;
     const float tx = fmaf(-w5, qx, fmaf(radial, dx, bx));
     const float ty = fmaf(-w5, qy, fmaf(radial, dy, by));

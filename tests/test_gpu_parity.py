@@ -334,3 +334,45 @@ def test_full_size_keys_perm_nodes(bh, orc):
         assert_acc_close(acc[tgt], ref_acc)
         direct = orc.direct(p2, m2, 0.005, targets=tgt[:512], nthreads=16)
         assert np.median(relerr(acc[tgt[:512]], direct)) <= 1e-3
+
+
+def _near_boundaries(rng, n, points):
+    """Float32 coordinates on, and 1 ulp either side of, the given FP64 boundary points."""
+    x = rng.choice(points, n).astype(np.float32)
+    side = rng.integers(-1, 2, n)
+    x = np.where(side > 0, np.nextafter(x, np.float32(np.inf)), x)
+    x = np.where(side < 0, np.nextafter(x, np.float32(-np.inf)), x)
+    return x
+
+
+@pytest.mark.parametrize("S,center,edge", [(1.0, (0.0, 0.0, 0.0), 2.0),
+                                           (0.7734375, (0.1, -0.3, 0.05), 2.6),
+                                           (3.3, (-1.25, 0.5, 2.0), 7.0)])
+def test_key_fast_paths_at_cell_boundaries(bh, orc, sim, S, center, edge):
+    """Morton and tree keys of coordinates sitting exactly on, or one float32 ulp beside, the
+    cell boundaries of the key grids (and some outside the cube): the FP32 fast paths must hand
+    every such coordinate to the exact FP64 path, so keys and the node set stay bit-exact."""
+    rng = np.random.default_rng(11)
+    n = 30000
+    frac = 2.0 ** 21 / (2.0 * S)
+    k = np.arange(-(1 << 21), (1 << 22) + 1, 97, dtype=np.float64)
+    morton_pts = k / frac - S  # (p + S) * frac = k
+    pm = np.zeros((n, 4), np.float32)
+    for a in range(3):
+        pm[:, a] = _near_boundaries(rng, n, morton_pts)
+    pm[:, 3] = rng.uniform(0.5, 1.5, n) / n
+    v = np.zeros_like(pm)
+    sim.set_bodies(pm, v)
+    keys = sim.morton_keys(S)
+    assert np.array_equal(keys, orc.morton_keys(pm[:, :3].astype(np.float64), S))
+    # tree-key comparison points: c0 + (k - 2^20) * edge / 2^21, k in [1, 2^21 - 1]
+    kt = np.arange(-64, (1 << 21) + 64, 61, dtype=np.float64)
+    for a in range(3):
+        pm[:, a] = _near_boundaries(rng, n, center[a] + (kt - 2.0 ** 20) * edge / 2.0 ** 21)
+    sim.set_bodies(pm, v)
+    pos, mass = pm[:, :3].astype(np.float64), pm[:, 3].astype(np.float64)
+    sim.build(np.array(center), edge, 4, bh.BH_MULTIPOLE_QUADRUPOLE)
+    t = sim.tree_nodes()
+    ref = orc.build(pos, mass, np.array(center), edge, 4, 1)
+    assert np.array_equal(t["keys"], ref["keys"])
+    assert np.array_equal(t["counts"], ref["counts"])
