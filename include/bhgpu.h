@@ -232,6 +232,23 @@ bh_status bh_measure_fp32_peak(bh_ctx* ctx, double* tflops);
 bh_status bh_sort_keys_static(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                               uint32_t* vals_out, size_t n, void* stream, uint32_t* status_out);
 
+/* Conservation diagnostics of the current state (no counterpart in the reference, which reports
+ * none). Kinetic energy, linear and angular momentum, mass and centre of mass are FP64 sums over
+ * the bodies; the potential energy 1/2 sum m_i phi_i takes phi from the current tree (built by
+ * bh_build or the last bh_step, over the current positions) with the reference's opening test at
+ * theta, softening eps and the tree's multipoles (theta = 0 gives the direct sum). pot_out
+ * (optional, n floats, slot order) receives phi. Returns BH_ERR_NO_TREE without a tree. */
+typedef struct bh_energy {
+  double kinetic;
+  double potential;
+  double total;
+  double momentum[3];
+  double angular_momentum[3];
+  double mass;
+  double com[3];
+} bh_energy;
+bh_status bh_energy_diag(bh_ctx* ctx, double theta, double eps, bh_energy* out, float* pot_out);
+
 /* Differentiable trajectory (reverse mode). The reference has no counterpart: it only
  * integrates forward (Simulation::run, src/Simulation.cpp). bh_adjoint_forward integrates
  * nsteps kick-drift-kick steps of the quadrupole tree force from the uploaded state (bodies

@@ -38,7 +38,7 @@ EXPORTS = [
     "bh_kick_drift", "bh_kick", "bh_step", "bh_params_default", "bh_synchronize", "bh_event_record",
     "bh_event_elapsed_ms", "bh_flush_l2", "bh_host_alloc", "bh_host_free", "bh_measure_fp32_peak",
     "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step", "bh_adjoint_forward",
-    "bh_step_backward",
+    "bh_step_backward", "bh_energy_diag",
 ]
 
 
@@ -70,6 +70,16 @@ class Stats(ctypes.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Energy(ctypes.Structure):
+    _fields_ = [("kinetic", ctypes.c_double), ("potential", ctypes.c_double), ("total", ctypes.c_double),
+                ("momentum", ctypes.c_double * 3), ("angular_momentum", ctypes.c_double * 3),
+                ("mass", ctypes.c_double), ("com", ctypes.c_double * 3)]
+
+    def as_dict(self):
+        return {k: (list(getattr(self, k)) if isinstance(getattr(self, k), ctypes.Array) else getattr(self, k))
+                for k, _ in self._fields_}
 
 
 class Node(ctypes.Structure):
@@ -125,6 +135,7 @@ def load():
         "bh_batch_step": ([P, ctypes.POINTER(Params), I, ctypes.POINTER(Stats)], I),
         "bh_adjoint_forward": ([P, ctypes.POINTER(Params), I, I, ctypes.POINTER(Stats)], I),
         "bh_step_backward": ([P, P, P, P, P, P, ctypes.POINTER(Stats)], I),
+        "bh_energy_diag": ([P, D, D, ctypes.POINTER(Energy), P], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -294,6 +305,13 @@ class Simulation:
         check(self.lib.bh_batch_step(self.h, ctypes.byref(params), nsteps, ctypes.byref(st) if stats else None),
               "bh_batch_step")
         return st
+
+    def energy(self, theta, eps, potential=False):
+        """Conservation diagnostics of the current state over the current tree (bh_energy_diag)."""
+        e = Energy()
+        pot = np.zeros(self.n, np.float32) if potential else None
+        check(self.lib.bh_energy_diag(self.h, theta, eps, ctypes.byref(e), _ptr(pot)), "bh_energy_diag")
+        return (e.as_dict(), pot) if potential else e.as_dict()
 
     def adjoint_forward(self, params, nsteps, checkpoint_every, stats=True):
         """Differentiable trajectory: nsteps KDK steps in upload order with checkpoints."""
