@@ -233,6 +233,22 @@ def cpu_sample(bh, w, pm, nthreads, walk_sample):
             "seconds_per_step": per_step}
 
 
+def cpu_steps_sample(systems, theta, eps, dt, leaf, edge, nthreads=1):
+    """Oracle port of one reference step (bounds, keys, sort, kick+drift, build, walk, kick) on
+    each (pos_m, vel) system given; returns the seconds of each."""
+    from oracle.oracle import Restatement
+
+    orc = Restatement()
+    out = []
+    for pm, vel in systems:
+        pos = pm[:, :3].astype(np.float64)
+        t0 = time.perf_counter()
+        orc.steps(pos, vel[:, :3].astype(np.float64), pm[:, 3].astype(np.float64), np.zeros_like(pos), dt, theta,
+                  eps, edge, leaf, 1, 1, acc_follows_body=1, nthreads=nthreads)
+        out.append(time.perf_counter() - t0)
+    return out
+
+
 def run_reference(args, w, dist):
     """CPU reference arm: the oracle port of the reference's step with all host threads."""
     if dist.rank != 0:
@@ -288,7 +304,10 @@ def run_ours(args, w, dist):
         sim.set_bodies(pm, vel)
 
     fp32_peak = sim.fp32_peak_tflops()
-    for _ in range(args.warmup):
+    # the first warm-up step builds a tree; the autotuner picks the walk's launch shape on it
+    sim.step(prm, 1, stats=False)
+    tune = sim.autotune(w["theta"], w["eps"], trials=3)
+    for _ in range(args.warmup - 1):
         sim.step(prm, 1, stats=False)
     sim.synchronize()
     energy0 = sim.energy(w["theta"], w["eps"])  # over the tree of the last warm-up step
@@ -398,6 +417,7 @@ def run_ours(args, w, dist):
         "wall_s_timed_loop": wall,
         "accuracy": accuracy,
         "conservation": conservation,
+        "autotune": tune,
     }
     if dist.rank == 0:
         clk = clocks.summary()
@@ -450,14 +470,18 @@ def run_ensemble(args, dist):
     sim = bh.Simulation(n)
     sim.batch_set(pos, vel, off)
     fp32_peak = sim.fp32_peak_tflops()
-    for _ in range(args.warmup):
+    sim.batch_step(prm, 1, stats=False)
+    tune = sim.autotune(e["theta"], e["eps"], trials=2)  # walk launch shape for this ensemble
+    for _ in range(args.warmup - 1):  # re-captures the step graph with the chosen walk
         sim.batch_step(prm, 1, stats=False)
     per_step, flops = [], []
+    launches = 0
     dist.barrier()
     with ClockSampler(int(os.environ.get("BH_GPU_INDEX", "0"))) as clocks:
         for _ in range(args.steps):
             sim.flush_l2()
             st = sim.batch_step(prm, 1)
+            launches += st.kernel_launches
             per_step.append(st.ms_step)
             flops.append(FLOPS_P2P * st.interactions_p2p + FLOPS_CELL_QUAD * st.interactions_cell)
     total_ms = dist.max(sum(per_step))
@@ -495,6 +519,19 @@ def run_ensemble(args, dist):
             loop_s.append(statistics.median(t))
     loop_step_s = sum(loop_s) * e["nsys"] / len(sample)
     walk_tflops = statistics.mean(flops) / (statistics.mean(per_step) * 1e-3) / 1e12
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        # the oracle port on one core over 12 seeded systems, scaled by sum N log N
+        sizes = np.diff(off).astype(np.float64)
+        pick = np.sort(np.random.default_rng(8).choice(e["nsys"], 12, replace=False))
+        secs = cpu_steps_sample([(pos[off[s]:off[s + 1]], vel[off[s]:off[s + 1]]) for s in pick], e["theta"],
+                                e["eps"], e["dt"], e["leaf"], e["edge"])
+        nlogn = sizes * np.log(sizes)
+        cpu_step_s = sum(secs) * float(nlogn.sum() / nlogn[pick].sum())
+        cpu = {"value": n / cpu_step_s, "unit": "body-steps/s", "cores": 1, "kind": "port",
+               "sample": f"one oracle-port step of 12 seeded systems ({sum(secs):.1f} s, "
+                         f"{int(sizes[pick].sum())} bodies), scaled by sum N log N to all {e['nsys']} systems: "
+                         f"{cpu_step_s:.0f} s per ensemble step"}
     if dist.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -509,7 +546,10 @@ def run_ensemble(args, dist):
                                          f"(median of 3), sum scaled by {e['nsys']}/{len(sample)}"},
                 "batched_speedup_vs_plain_loop": loop_step_s / (total_ms / args.steps * 1e-3),
                 "flops_per_step": statistics.mean(flops), "tflops": walk_tflops,
-                "fp32_peak_tflops": fp32_peak, "clocks": clocks.summary()}
+                "fp32_peak_tflops": fp32_peak, "gpu_launches": launches, "autotune": tune,
+                "clocks": clocks.summary()}
+        if cpu:
+            line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
 
 
@@ -588,6 +628,13 @@ def run_adjoint(args, dist):
         x.free()
     sim.close()
     plain_ms = statistics.median(plain)
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        secs = cpu_steps_sample([(pm, vel)] * 2, a["theta"], a["eps"], a["dt"], a["leaf"], a["edge"])
+        per = statistics.mean(secs)
+        cpu = {"value": n / per, "unit": "body-steps/s (forward only)", "cores": 1, "kind": "port",
+               "sample": f"two oracle-port forward steps of the N={n} system ({sum(secs):.1f} s); the reference "
+                         f"has no reverse mode, so this is its forward cost per step"}
     if dist.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "body-steps/s (differentiated)", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -608,6 +655,8 @@ def run_adjoint(args, dist):
                         "h2d_bytes_per_step": 48 * n, "d2h_bytes_per_step": 32 * n + 36 * n,
                         "ms_per_step": statistics.median(e2e)},
                 "gpu_launches": launches, "clocks": clocks.summary()}
+        if cpu:
+            line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
 
 

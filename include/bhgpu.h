@@ -232,6 +232,26 @@ bh_status bh_measure_fp32_peak(bh_ctx* ctx, double* tflops);
 bh_status bh_sort_keys_static(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                               uint32_t* vals_out, size_t n, void* stream, uint32_t* status_out);
 
+/* Walk autotuner (no counterpart in the reference, whose walk is one serial loop). Times each
+ * launch shape of the quadrupole tree walk (warps per block, register budget as resident blocks
+ * per SM, per-warp stack depth; groups are always the 32 bodies of one warp, one per lane, since
+ * the per-lane opening masks are 32-bit) on the tree currently in the context: the last
+ * bh_step / bh_build, or the last bh_batch_step of an ensemble. Each shape runs `trials` timed
+ * force-only walks after one warm-up (the state is not changed); the fastest median becomes the
+ * context's walk for quadrupole steps with eps > 0. Shapes whose stack cannot hold the tree get
+ * ms = -1. */
+#define BH_TUNE_MAX_VARIANTS 8
+typedef struct bh_tune_result {
+  int variants;
+  int best;
+  int warps_per_block[BH_TUNE_MAX_VARIANTS];
+  int min_blocks_per_sm[BH_TUNE_MAX_VARIANTS];
+  int stack_depth[BH_TUNE_MAX_VARIANTS];
+  int registers[BH_TUNE_MAX_VARIANTS];
+  float ms[BH_TUNE_MAX_VARIANTS];
+} bh_tune_result;
+bh_status bh_autotune_walk(bh_ctx* ctx, double theta, double eps, int trials, bh_tune_result* out);
+
 /* Conservation diagnostics of the current state (no counterpart in the reference, which reports
  * none). Kinetic energy, linear and angular momentum, mass and centre of mass are FP64 sums over
  * the bodies; the potential energy 1/2 sum m_i phi_i takes phi from the current tree (built by

@@ -38,7 +38,7 @@ EXPORTS = [
     "bh_kick_drift", "bh_kick", "bh_step", "bh_params_default", "bh_synchronize", "bh_event_record",
     "bh_event_elapsed_ms", "bh_flush_l2", "bh_host_alloc", "bh_host_free", "bh_measure_fp32_peak",
     "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step", "bh_adjoint_forward",
-    "bh_step_backward", "bh_energy_diag",
+    "bh_step_backward", "bh_energy_diag", "bh_autotune_walk",
 ]
 
 
@@ -80,6 +80,19 @@ class Energy(ctypes.Structure):
     def as_dict(self):
         return {k: (list(getattr(self, k)) if isinstance(getattr(self, k), ctypes.Array) else getattr(self, k))
                 for k, _ in self._fields_}
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("variants", ctypes.c_int), ("best", ctypes.c_int), ("warps_per_block", ctypes.c_int * 8),
+                ("min_blocks_per_sm", ctypes.c_int * 8), ("stack_depth", ctypes.c_int * 8),
+                ("registers", ctypes.c_int * 8), ("ms", ctypes.c_float * 8)]
+
+    def as_dict(self):
+        k = self.variants
+        return {"best": self.best,
+                "variants": [{"warps_per_block": self.warps_per_block[i], "min_blocks_per_sm": self.min_blocks_per_sm[i],
+                              "stack_depth": self.stack_depth[i], "registers": self.registers[i], "ms": self.ms[i]}
+                             for i in range(k)]}
 
 
 class Node(ctypes.Structure):
@@ -136,6 +149,7 @@ def load():
         "bh_adjoint_forward": ([P, ctypes.POINTER(Params), I, I, ctypes.POINTER(Stats)], I),
         "bh_step_backward": ([P, P, P, P, P, P, ctypes.POINTER(Stats)], I),
         "bh_energy_diag": ([P, D, D, ctypes.POINTER(Energy), P], I),
+        "bh_autotune_walk": ([P, D, D, I, ctypes.POINTER(TuneResult)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -305,6 +319,12 @@ class Simulation:
         check(self.lib.bh_batch_step(self.h, ctypes.byref(params), nsteps, ctypes.byref(st) if stats else None),
               "bh_batch_step")
         return st
+
+    def autotune(self, theta, eps, trials=3):
+        """Times the walk's launch shapes on the current tree and keeps the fastest (bh_autotune_walk)."""
+        r = TuneResult()
+        check(self.lib.bh_autotune_walk(self.h, theta, eps, trials, ctypes.byref(r)), "bh_autotune_walk")
+        return r.as_dict()
 
     def energy(self, theta, eps, potential=False):
         """Conservation diagnostics of the current state over the current tree (bh_energy_diag)."""

@@ -279,6 +279,7 @@ bh_status bh_set_state(bh_ctx* c, const float* pos_m4, const float* vel4, const 
   c->cur = 0;
   c->tree_valid = false;
   c->batch = false;
+  c->batch_tree_ready = false;
   bh::adj_invalidate(c);
   for (auto& g : c->graph)
     if (g) {
@@ -873,7 +874,64 @@ bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* s
   if (st) st->kernel_launches = (uint32_t)(c->launches - launches0);
   c->tree_valid = false;  // the ensemble's tree is not a single-system tree
   c->hash_valid = false;
+  c->batch_tree_ready = nsteps > 0;
   return last_launch();
+}
+
+// Times every launch shape of the quadrupole walk on the tree in the arena (the last bh_step /
+// bh_build, or the last bh_batch_step) and keeps the fastest for this context.
+bh_status bh_autotune_walk(bh_ctx* c, double theta, double eps, int trials, bh_tune_result* out) {
+  if (!c || !out || !(theta >= 0) || !(eps > 0) || trials < 1) return BH_ERR_INVALID_ARG;
+  const bool batch = c->batch;
+  if (batch ? !c->batch_tree_ready : !c->tree_valid) return BH_ERR_NO_TREE;
+  cudaSetDevice(c->device);
+  std::memset(out, 0, sizeof(*out));
+  const int n = (int)c->n;
+  const int nv = std::min(bh::walk_variants(), (int)BH_TUNE_MAX_VARIANTS);
+  float4* scratch = nullptr;
+  BH_TRY(dalloc(&scratch, c->n));
+  bh_status status = BH_OK;
+  float best_ms = 0.f;
+  int best = 0;
+  for (int v = 0; v < nv; ++v) {
+    const bh::WalkVariant info = bh::walk_variant_info(v);
+    out->warps_per_block[v] = info.warps;
+    out->min_blocks_per_sm[v] = info.min_blocks;
+    out->stack_depth[v] = info.stack;
+    out->registers[v] = info.regs;
+    std::vector<float> ms;
+    uint32_t e = 0;
+    for (int t = 0; t <= trials && e == 0; ++t) {  // trial 0 warms up
+      clear_device_flags(c);
+      cudaEventRecord(c->stage_ev[0], c->stream);
+      bh::launch_walk_variant(c, v, n, (float)theta, (float)eps, scratch, batch);
+      cudaEventRecord(c->stage_ev[1], c->stream);
+      status = last_launch();
+      if (status == BH_OK) status = sync_and_check(c, &e);
+      if (status != BH_OK) break;
+      if (t > 0) ms.push_back(elapsed(c, 0, 1));
+    }
+    if (status != BH_OK) break;
+    if (e || ms.empty()) {  // this shape cannot run the tree (stack): never chosen
+      out->ms[v] = -1.f;
+      continue;
+    }
+    std::sort(ms.begin(), ms.end());
+    out->ms[v] = ms[ms.size() / 2];
+    if (best_ms == 0.f || out->ms[v] < best_ms) {
+      best_ms = out->ms[v];
+      best = v;
+    }
+  }
+  dfree(scratch);
+  BH_TRY(status);
+  if (best_ms == 0.f) return BH_ERR_OVERFLOW_STACK;
+  out->variants = nv;
+  out->best = best;
+  if (c->walk_variant != best) destroy_graphs(c);  // captured batched steps hold the old kernel
+  c->walk_variant = best;
+  clear_device_flags(c);
+  return BH_OK;
 }
 
 }  // extern "C"

@@ -170,6 +170,9 @@ struct bh_ctx {
   uint64_t launches = 0;  // kernels launched on this context (every launcher adds its count)
 
   void* adj = nullptr;  // differentiable-path state (checkpoints, tape, adjoints): bh_adjoint.cu
+
+  int walk_variant = 0;           // launch shape of the quadrupole walk (bh_autotune_walk)
+  bool batch_tree_ready = false;  // the arena holds the tree of the last batched step
 };
 
 namespace bh {
@@ -242,6 +245,14 @@ void launch_lookup(bh_ctx* c, uint64_t key, int* out_index);
 void launch_walk_record(bh_ctx* c, int n, float theta, float eps, float4* acc_slot, float4* vel_kick, float half_dt,
                         Chunk* tape, unsigned* tape_count, int tape_cap);
 void launch_fp32_peak(cudaStream_t st, float* sink, int blocks);
+// Launch shapes of the quadrupole walk (positive softening) that bh_autotune_walk times.
+struct WalkVariant {
+  int warps, min_blocks, stack, regs;
+};
+int walk_variants();
+WalkVariant walk_variant_info(int v);
+void launch_walk_variant(bh_ctx* c, int v, int n, float theta, float eps, float4* acc_out, bool batch);
+
 // Frees the differentiable-path state of the context.
 void adj_release(bh_ctx* c);
 // Marks the recorded trajectory stale (new bodies were uploaded).

@@ -33,15 +33,28 @@
 namespace bh {
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kWarps = kThreads / 32;
-constexpr int kStack = 384;
-constexpr int kStackDeep = 160;  // above this depth the warp pops one entry per round (DFS bound)
 constexpr int kBuf = 64;
 constexpr uint32_t kChildShift = 28;  // stack entry: first_child | nchild << 28
 constexpr float kMacMargin = 1e-5f;
 
-struct WarpSmem {
+// Launch shape of one walk variant: warps per block, resident blocks per SM the register
+// allocation must allow, and the per-warp stack depth. Above
+// kStack - 224 entries the warp pops one entry per round, so a full round (at most 7 new
+// entries per level of the remaining depth) always fits.
+template <int kBlockWarps, int kMinBlocksPerSM, int kStackDepth>
+struct WalkCfg {
+  static constexpr int kWarps = kBlockWarps;
+  static constexpr int kThreads = 32 * kBlockWarps;
+  static constexpr int kMinBlocks = kMinBlocksPerSM;
+  static constexpr int kStack = kStackDepth;
+  static constexpr int kStackDeep = kStackDepth - 224;
+};
+using CfgDefault = WalkCfg<8, 4, 384>;
+constexpr int kThreads = CfgDefault::kThreads;
+constexpr int kWarps = CfgDefault::kWarps;
+
+template <int kStack>
+struct WarpSmemT {
   uint32_t stk_node[kStack];
   uint32_t stk_mask[kStack];
   int cell_node[kBuf];
@@ -101,8 +114,8 @@ __device__ __forceinline__ void record_chunk(const Rec& r, int kind, int cnt, co
 }
 
 // 32 multipole cells (monopole + quadrupole). The lane mask rides in st2.w.
-template <bool kRec>
-__device__ __forceinline__ void eval_cells(WarpSmem& s, int cnt, const WalkNode* __restrict__ nodes,
+template <bool kRec, class Smem>
+__device__ __forceinline__ void eval_cells(Smem& s, int cnt, const WalkNode* __restrict__ nodes,
                                            uint32_t lanebit, float px, float py, float pz, float eps2, Acc& acc,
                                            unsigned long long& ev, const Rec& rec) {
   ev += (unsigned)cnt;
@@ -149,8 +162,8 @@ __device__ __forceinline__ void eval_cells(WarpSmem& s, int cnt, const WalkNode*
 }
 
 // Up to 32 point masses. The lane mask is read from pt_mask.
-template <bool kSelfTest, bool kRec>
-__device__ __forceinline__ void eval_points(WarpSmem& s, int cnt, const WalkNode* __restrict__ nodes,
+template <bool kSelfTest, bool kRec, class Smem>
+__device__ __forceinline__ void eval_points(Smem& s, int cnt, const WalkNode* __restrict__ nodes,
                                             const float4* __restrict__ tpos, uint32_t lanebit, float px, float py,
                                             float pz, float eps2, Acc& acc, unsigned long long& ev, const Rec& rec) {
   ev += (unsigned)cnt;
@@ -207,8 +220,8 @@ __device__ __forceinline__ void shift_down(int* idx, uint32_t* msk, int n, int l
   }
 }
 
-template <bool kQuad, bool kSelfTest, bool kRec = false>
-__global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ nodes,
+template <bool kQuad, bool kSelfTest, bool kRec = false, class Cfg = CfgDefault>
+__global__ __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) void k_walk(const WalkNode* __restrict__ nodes,
                                                    const float4* __restrict__ tpos,
                                                    const uint32_t* __restrict__ tslot, int n, float theta2,
                                                    float eps2, float4* __restrict__ acc_slot,
@@ -217,11 +230,12 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
                                                    Counters* __restrict__ ctr, uint32_t* __restrict__ err,
                                                    Chunk* __restrict__ tape = nullptr,
                                                    unsigned* __restrict__ tape_count = nullptr, int tape_cap = 0) {
-  __shared__ WarpSmem smem[kWarps];
+  constexpr int kStack = Cfg::kStack, kStackDeep = Cfg::kStackDeep;
+  __shared__ WarpSmemT<kStack> smem[Cfg::kWarps];
   const int lane = threadIdx.x & 31;
   const uint32_t lanebit = 1u << lane;
   const uint32_t lt_mask = lanebit - 1u;
-  WarpSmem& s = smem[threadIdx.x >> 5];
+  WarpSmemT<kStack>& s = smem[threadIdx.x >> 5];
   if (*((volatile uint32_t*)err) & (kErrNodes | kErrTimeout)) return;
   // work items: groups of up to 32 consecutive bodies (tree order) under one root. Without a
   // group table, group g is bodies [32 g, 32 g + 32) of the single tree rooted at node 0;
@@ -516,37 +530,94 @@ __global__ __launch_bounds__(kThreads) void k_walk(const WalkNode* __restrict__ 
   }
 }
 
-template <bool kQuad, bool kSelf>
+// Persistent grid of one walk instantiation: every block that can be resident at once.
+template <bool kQuad, bool kSelf, bool kRec, class Cfg>
 int walk_grid() {
   static int blocks = 0;
   if (blocks == 0) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<kQuad, kSelf>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<kQuad, kSelf, kRec, Cfg>, Cfg::kThreads, 0);
     blocks = max(1, sms * max(1, per_sm));
   }
   return blocks;
 }
 
-template <bool kQuad, bool kSelf>
+template <bool kQuad, bool kSelf, class Cfg = CfgDefault>
 void launch_walk_t(bh_ctx* c, int n, float theta2, float eps2, float4* acc_slot, float4* vel_kick, float half_dt,
                    bool batch) {
   const int ngroups = batch ? c->ngroups : (n + 31) / 32;
-  const int grid = min(walk_grid<kQuad, kSelf>(), ngroups / kWarps + 1);
-  k_walk<kQuad, kSelf><<<grid, kThreads, 0, c->stream>>>(c->wnode, c->tpos, c->tslot, n, theta2, eps2, acc_slot,
-                                                         vel_kick, half_dt, batch ? c->groups : nullptr,
-                                                         c->ngroups, c->counters, c->err);
+  const int grid = min(walk_grid<kQuad, kSelf, false, Cfg>(), ngroups / Cfg::kWarps + 1);
+  k_walk<kQuad, kSelf, false, Cfg><<<grid, Cfg::kThreads, 0, c->stream>>>(
+      c->wnode, c->tpos, c->tslot, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch ? c->groups : nullptr,
+      c->ngroups, c->counters, c->err);
+}
+
+// Launch shapes the autotuner chooses from for the quadrupole walk with positive softening
+// (the benchmarked path): block size, register budget (resident blocks per SM) and stack depth.
+// Static shared memory caps a block at 48 KB, which bounds warps x stack depth.
+using Cfg1 = WalkCfg<8, 3, 384>;
+using Cfg2 = WalkCfg<8, 2, 384>;
+using Cfg3 = WalkCfg<4, 8, 384>;
+using Cfg4 = WalkCfg<4, 6, 384>;
+using Cfg5 = WalkCfg<4, 8, 512>;
+constexpr int kVariants = 6;
+
+template <class Cfg>
+WalkVariant variant_info() {
+  cudaFuncAttributes fa{};
+  cudaFuncGetAttributes(&fa, k_walk<true, false, false, Cfg>);
+  return {Cfg::kWarps, Cfg::kMinBlocks, Cfg::kStack, fa.numRegs};
+}
+
+void launch_quad_variant(bh_ctx* c, int v, int n, float theta2, float eps2, float4* acc_slot, float4* vel_kick,
+                         float half_dt, bool batch) {
+  switch (v) {
+    case 1: launch_walk_t<true, false, Cfg1>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
+    case 2: launch_walk_t<true, false, Cfg2>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
+    case 3: launch_walk_t<true, false, Cfg3>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
+    case 4: launch_walk_t<true, false, Cfg4>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
+    case 5: launch_walk_t<true, false, Cfg5>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
+    default: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
+  }
 }
 
 }  // namespace
 
+int walk_variants() { return kVariants; }
+
+WalkVariant walk_variant_info(int v) {
+  switch (v) {
+    case 1: return variant_info<Cfg1>();
+    case 2: return variant_info<Cfg2>();
+    case 3: return variant_info<Cfg3>();
+    case 4: return variant_info<Cfg4>();
+    case 5: return variant_info<Cfg5>();
+    default: return variant_info<CfgDefault>();
+  }
+}
+
+// One force-only walk with the given variant (the autotuner's trial); acc_out by slot.
+void launch_walk_variant(bh_ctx* c, int v, int n, float theta, float eps, float4* acc_out, bool batch) {
+  if (n <= 0) return;
+  cudaMemsetAsync(&c->counters->group_next, 0, sizeof(unsigned), c->stream);
+  c->launches += 1;
+  launch_quad_variant(c, v, n, theta * theta, eps * eps, acc_out, nullptr, 0.f, batch);
+}
+
 // Occupancy queries done once per process, before any stream capture.
 void walk_init() {
-  walk_grid<true, true>();
-  walk_grid<true, false>();
-  walk_grid<false, true>();
-  walk_grid<false, false>();
+  walk_grid<true, true, false, CfgDefault>();
+  walk_grid<true, false, false, CfgDefault>();
+  walk_grid<false, true, false, CfgDefault>();
+  walk_grid<false, false, false, CfgDefault>();
+  walk_grid<true, false, true, CfgDefault>();
+  walk_grid<true, false, false, Cfg1>();
+  walk_grid<true, false, false, Cfg2>();
+  walk_grid<true, false, false, Cfg3>();
+  walk_grid<true, false, false, Cfg4>();
+  walk_grid<true, false, false, Cfg5>();
 }
 
 void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc_slot, float4* vel_kick,
@@ -561,7 +632,7 @@ void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc
     if (self)
       launch_walk_t<true, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
     else
-      launch_walk_t<true, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
+      launch_quad_variant(c, c->walk_variant, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
   } else {
     if (self)
       launch_walk_t<false, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
@@ -582,7 +653,7 @@ void launch_walk_record(bh_ctx* c, int n, float theta, float eps, float4* acc_sl
   if (n <= 0) return;
   cudaMemsetAsync(&c->counters->group_next, 0, sizeof(unsigned), c->stream);
   c->launches += 1;
-  const int grid = min(walk_grid<true, false>(), ((n + 31) / 32) / kWarps + 1);
+  const int grid = min(walk_grid<true, false, true, CfgDefault>(), ((n + 31) / 32) / kWarps + 1);
   k_walk<true, false, true><<<grid, kThreads, 0, c->stream>>>(c->wnode, c->tpos, c->tslot, n, theta * theta,
                                                               eps * eps, acc_slot, vel_kick, half_dt, nullptr, 0,
                                                               c->counters, c->err, tape, tape_count, tape_cap);
