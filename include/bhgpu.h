@@ -247,10 +247,13 @@ typedef struct bh_tune_result {
   int warps_per_block[BH_TUNE_MAX_VARIANTS];
   int min_blocks_per_sm[BH_TUNE_MAX_VARIANTS];
   int stack_depth[BH_TUNE_MAX_VARIANTS];
+  int cell_form[BH_TUNE_MAX_VARIANTS]; /* 0: three selects per cell; 1: one select on the common factor */
   int registers[BH_TUNE_MAX_VARIANTS];
   float ms[BH_TUNE_MAX_VARIANTS];
 } bh_tune_result;
 bh_status bh_autotune_walk(bh_ctx* ctx, double theta, double eps, int trials, bh_tune_result* out);
+/* Pins the walk's launch shape (an index of bh_tune_result, 0 = the default) without timing. */
+bh_status bh_set_walk_variant(bh_ctx* ctx, int variant);
 
 /* Conservation diagnostics of the current state (no counterpart in the reference, which reports
  * none). Kinetic energy, linear and angular momentum, mass and centre of mass are FP64 sums over

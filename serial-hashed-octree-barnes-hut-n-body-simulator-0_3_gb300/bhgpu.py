@@ -38,7 +38,7 @@ EXPORTS = [
     "bh_kick_drift", "bh_kick", "bh_step", "bh_params_default", "bh_synchronize", "bh_event_record",
     "bh_event_elapsed_ms", "bh_flush_l2", "bh_host_alloc", "bh_host_free", "bh_measure_fp32_peak",
     "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step", "bh_adjoint_forward",
-    "bh_step_backward", "bh_energy_diag", "bh_autotune_walk",
+    "bh_step_backward", "bh_energy_diag", "bh_autotune_walk", "bh_set_walk_variant",
 ]
 
 
@@ -85,13 +85,14 @@ class Energy(ctypes.Structure):
 class TuneResult(ctypes.Structure):
     _fields_ = [("variants", ctypes.c_int), ("best", ctypes.c_int), ("warps_per_block", ctypes.c_int * 8),
                 ("min_blocks_per_sm", ctypes.c_int * 8), ("stack_depth", ctypes.c_int * 8),
-                ("registers", ctypes.c_int * 8), ("ms", ctypes.c_float * 8)]
+                ("cell_form", ctypes.c_int * 8), ("registers", ctypes.c_int * 8), ("ms", ctypes.c_float * 8)]
 
     def as_dict(self):
         k = self.variants
         return {"best": self.best,
                 "variants": [{"warps_per_block": self.warps_per_block[i], "min_blocks_per_sm": self.min_blocks_per_sm[i],
-                              "stack_depth": self.stack_depth[i], "registers": self.registers[i], "ms": self.ms[i]}
+                              "stack_depth": self.stack_depth[i], "cell_form": self.cell_form[i],
+                              "registers": self.registers[i], "ms": self.ms[i]}
                              for i in range(k)]}
 
 
@@ -150,6 +151,7 @@ def load():
         "bh_step_backward": ([P, P, P, P, P, P, ctypes.POINTER(Stats)], I),
         "bh_energy_diag": ([P, D, D, ctypes.POINTER(Energy), P], I),
         "bh_autotune_walk": ([P, D, D, I, ctypes.POINTER(TuneResult)], I),
+        "bh_set_walk_variant": ([P, I], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -325,6 +327,9 @@ class Simulation:
         r = TuneResult()
         check(self.lib.bh_autotune_walk(self.h, theta, eps, trials, ctypes.byref(r)), "bh_autotune_walk")
         return r.as_dict()
+
+    def set_walk_variant(self, v):
+        check(self.lib.bh_set_walk_variant(self.h, v), "bh_set_walk_variant")
 
     def energy(self, theta, eps, potential=False):
         """Conservation diagnostics of the current state over the current tree (bh_energy_diag)."""

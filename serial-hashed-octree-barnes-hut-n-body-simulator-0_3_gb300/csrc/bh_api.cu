@@ -898,6 +898,7 @@ bh_status bh_autotune_walk(bh_ctx* c, double theta, double eps, int trials, bh_t
     out->warps_per_block[v] = info.warps;
     out->min_blocks_per_sm[v] = info.min_blocks;
     out->stack_depth[v] = info.stack;
+    out->cell_form[v] = info.form;
     out->registers[v] = info.regs;
     std::vector<float> ms;
     uint32_t e = 0;
@@ -931,6 +932,14 @@ bh_status bh_autotune_walk(bh_ctx* c, double theta, double eps, int trials, bh_t
   if (c->walk_variant != best) destroy_graphs(c);  // captured batched steps hold the old kernel
   c->walk_variant = best;
   clear_device_flags(c);
+  return BH_OK;
+}
+
+bh_status bh_set_walk_variant(bh_ctx* c, int variant) {
+  if (!c || variant < 0 || variant >= std::min(bh::walk_variants(), (int)BH_TUNE_MAX_VARIANTS))
+    return BH_ERR_INVALID_ARG;
+  if (c->walk_variant != variant) destroy_graphs(c);
+  c->walk_variant = variant;
   return BH_OK;
 }
 

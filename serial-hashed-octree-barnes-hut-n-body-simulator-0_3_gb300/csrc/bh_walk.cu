@@ -41,8 +41,9 @@ constexpr float kMacMargin = 1e-5f;
 // allocation must allow, and the per-warp stack depth. Above
 // kStack - 224 entries the warp pops one entry per round, so a full round (at most 7 new
 // entries per level of the remaining depth) always fits.
-template <int kBlockWarps, int kMinBlocksPerSM, int kStackDepth>
+template <int kBlockWarps, int kMinBlocksPerSM, int kStackDepth, int kCellForm = 0>
 struct WalkCfg {
+  static constexpr int kForm = kCellForm;  // cell evaluation form (eval_cells)
   static constexpr int kWarps = kBlockWarps;
   static constexpr int kThreads = 32 * kBlockWarps;
   static constexpr int kMinBlocks = kMinBlocksPerSM;
@@ -114,7 +115,7 @@ __device__ __forceinline__ void record_chunk(const Rec& r, int kind, int cnt, co
 }
 
 // 32 multipole cells (monopole + quadrupole). The lane mask rides in st2.w.
-template <bool kRec, class Smem>
+template <bool kRec, int kForm = 0, class Smem>
 __device__ __forceinline__ void eval_cells(Smem& s, int cnt, const WalkNode* __restrict__ nodes,
                                            uint32_t lanebit, float px, float py, float pz, float eps2, Acc& acc,
                                            unsigned long long& ev, const Rec& rec) {
@@ -148,15 +149,23 @@ __device__ __forceinline__ void eval_cells(Smem& s, int cnt, const WalkNode* __r
     const float qr = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
     // a += d (m / D^3 + 2.5 (d.Q.d) / D^7) - Q.d / D^5
     const float radial = fmaf(qr, w5 * (2.5f * u), c1.x * w3);
-    // selects rather than a branch: every lane runs the same straight-line code (a select on
-    // 1/D instead, zeroing every term, puts the select on the dependent chain and runs slower)
+    // selects rather than a branch: every lane runs the same straight-line code
     const bool take = (__float_as_uint(c2.w) & lanebit) != 0u;
-    const float tx = fmaf(-w5, qx, fmaf(radial, dx, bx));
-    const float ty = fmaf(-w5, qy, fmaf(radial, dy, by));
-    const float tz = fmaf(-w5, qz, fmaf(radial, dz, bz));
-    bx = take ? tx : bx;
-    by = take ? ty : by;
-    bz = take ? tz : bz;
+    if (kForm == 0) {
+      const float tx = fmaf(-w5, qx, fmaf(radial, dx, bx));
+      const float ty = fmaf(-w5, qy, fmaf(radial, dy, by));
+      const float tz = fmaf(-w5, qz, fmaf(radial, dz, bz));
+      bx = take ? tx : bx;
+      by = take ? ty : by;
+      bz = take ? tz : bz;
+    } else {
+      // a = w5 ((m D^2 + 2.5 (d.Q.d) / D^2) d - Q.d): one select zeroes the common factor
+      const float k = fmaf(2.5f * u, qr, c1.x * r2);
+      const float w5m = take ? w5 : 0.f;
+      bx = fmaf(w5m, fmaf(k, dx, -qx), bx);
+      by = fmaf(w5m, fmaf(k, dy, -qy), by);
+      bz = fmaf(w5m, fmaf(k, dz, -qz), bz);
+    }
   }
   acc.add(bx, by, bz);
 }
@@ -402,7 +411,7 @@ __global__ __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) void k_walk(const W
           }
           ncell += __popc(bal);
           if (ncell >= 32) {
-            eval_cells<kRec>(s,32, nodes, lanebit, p.x, p.y, p.z, eps2, acc, ev_cell, rec);
+            eval_cells<kRec, Cfg::kForm>(s,32, nodes, lanebit, p.x, p.y, p.z, eps2, acc, ev_cell, rec);
             shift_down(s.cell_node, s.cell_mask, ncell, lane);
             ncell -= 32;
           }
@@ -494,7 +503,7 @@ __global__ __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) void k_walk(const W
         }
       }
     }
-    if (ncell > 0) eval_cells<kRec>(s,ncell, nodes, lanebit, p.x, p.y, p.z, eps2, acc, ev_cell, rec);
+    if (ncell > 0) eval_cells<kRec, Cfg::kForm>(s,ncell, nodes, lanebit, p.x, p.y, p.z, eps2, acc, ev_cell, rec);
     if (npt > 0) eval_points<kSelfTest, kRec>(s,npt, nodes, tpos, lanebit, p.x, p.y, p.z, eps2, acc, ev_pt, rec);
     if (valid) {
       const uint32_t slot = __ldg(tslot + i);
@@ -562,13 +571,15 @@ using Cfg2 = WalkCfg<8, 2, 384>;
 using Cfg3 = WalkCfg<4, 8, 384>;
 using Cfg4 = WalkCfg<4, 6, 384>;
 using Cfg5 = WalkCfg<4, 8, 512>;
-constexpr int kVariants = 6;
+using Cfg6 = WalkCfg<8, 4, 384, 1>;
+using Cfg7 = WalkCfg<4, 8, 384, 1>;
+constexpr int kVariants = 8;
 
 template <class Cfg>
 WalkVariant variant_info() {
   cudaFuncAttributes fa{};
   cudaFuncGetAttributes(&fa, k_walk<true, false, false, Cfg>);
-  return {Cfg::kWarps, Cfg::kMinBlocks, Cfg::kStack, fa.numRegs};
+  return {Cfg::kWarps, Cfg::kMinBlocks, Cfg::kStack, Cfg::kForm, fa.numRegs};
 }
 
 void launch_quad_variant(bh_ctx* c, int v, int n, float theta2, float eps2, float4* acc_slot, float4* vel_kick,
@@ -579,6 +590,8 @@ void launch_quad_variant(bh_ctx* c, int v, int n, float theta2, float eps2, floa
     case 3: launch_walk_t<true, false, Cfg3>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
     case 4: launch_walk_t<true, false, Cfg4>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
     case 5: launch_walk_t<true, false, Cfg5>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
+    case 6: launch_walk_t<true, false, Cfg6>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
+    case 7: launch_walk_t<true, false, Cfg7>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
     default: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
   }
 }
@@ -594,6 +607,8 @@ WalkVariant walk_variant_info(int v) {
     case 3: return variant_info<Cfg3>();
     case 4: return variant_info<Cfg4>();
     case 5: return variant_info<Cfg5>();
+    case 6: return variant_info<Cfg6>();
+    case 7: return variant_info<Cfg7>();
     default: return variant_info<CfgDefault>();
   }
 }
@@ -618,6 +633,8 @@ void walk_init() {
   walk_grid<true, false, false, Cfg3>();
   walk_grid<true, false, false, Cfg4>();
   walk_grid<true, false, false, Cfg5>();
+  walk_grid<true, false, false, Cfg6>();
+  walk_grid<true, false, false, Cfg7>();
 }
 
 void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc_slot, float4* vel_kick,

@@ -53,3 +53,29 @@ def test_autotune_batched_then_step(bh):
             out.append(sim.get_bodies())
     assert np.allclose(out[0][0], out[1][0], rtol=0, atol=1e-5)
     assert float(np.median(relerr(out[0][2], out[1][2]))) < 1e-5
+
+
+@pytest.mark.parametrize("variant", range(8))
+def test_every_walk_variant_matches_oracle(bh, orc, variant):
+    """Each launch shape (and cell-evaluation form) the tuner can pick gives the reference's
+    interaction sets and accelerations within the parity bars."""
+    n = 20000
+    pm, vel = bh.plummer(9, n)
+    with bh.Simulation(n) as sim:
+        sim.set_bodies(pm, vel)
+        sim.set_walk_variant(variant)
+        c, size = sim.bounds()
+        sim.build(c, 2 * size, 8, bh.BH_MULTIPOLE_QUADRUPOLE)
+        acc, st = sim.force(0.5, 0.01, stats=True)
+        p, _, _ = sim.get_bodies()
+    pos, mass = p[:, :3].astype(np.float64), p[:, 3].astype(np.float64)
+    ref, ncell, npt = orc.force(pos, mass, c, 2 * size, 8, 1, 0.5, 0.01, nthreads=8)
+    err = relerr(acc, ref)
+    assert float(np.median(err)) <= 1e-5 and float(np.percentile(err, 99)) <= 1e-4
+    assert abs(st.interactions_cell - int(ncell.sum())) <= 1e-4 * ncell.sum()
+
+
+def test_set_walk_variant_rejects_out_of_range(bh):
+    with bh.Simulation(10) as sim:
+        with pytest.raises(bh.BHError):
+            sim.set_walk_variant(99)
