@@ -290,6 +290,30 @@ bh_status bh_adjoint_forward(bh_ctx* ctx, const bh_params* params, int nsteps, i
 bh_status bh_step_backward(bh_ctx* ctx, const float* dloss_dpos4, const float* dloss_dvel4, float* grad_pos4,
                            float* grad_vel4, float* grad_mass, bh_stats* stats);
 
+/* Initial conditions generated on the device (no counterpart in the reference, which builds its
+ * bodies on the host): a Plummer sphere by the recipe of bh_plummer (G = 1, scale radius a,
+ * total mass mtot, r > 10 a rejected, centre-of-mass frame, then the optional offsets), drawn
+ * with a counter-based generator per body, so the samples differ from bh_plummer's but follow
+ * the same distribution; the state of the context becomes these n bodies (like bh_set_bodies).
+ * bh_batch_plummer_device fills an ensemble (like bh_batch_set): system s gets the Plummer
+ * sphere of seed + s with sys_offsets[s+1] - sys_offsets[s] bodies, a and mtot each. */
+bh_status bh_plummer_device(bh_ctx* ctx, uint64_t seed, size_t n, double a, double mtot,
+                            const double* pos_offset3, const double* vel_offset3);
+bh_status bh_batch_plummer_device(bh_ctx* ctx, uint64_t seed, const uint32_t* sys_offsets, size_t nsys,
+                                  double a, double mtot);
+
+/* Headless stand-in for the reference's node-box drawing (visualizeTree,
+ * src/HashedOctree.cpp:939-974): for every node of the current tree (bh_build or the last
+ * bh_step; node order of bh_tree_nodes) its cube as (centre x, y, z, edge), its depth and its
+ * body count. Each output may be null; cap must be at least bh_tree_size. */
+bh_status bh_tree_boxes(bh_ctx* ctx, size_t cap, float* center_edge4, int32_t* depth, int64_t* count);
+
+/* Snapshot files (no counterpart in the reference): the bodies (slot order), their
+ * accelerations (so a run continues its leapfrog exactly) and, for an ensemble, the system
+ * offsets. Loading replaces the context's state like bh_set_state / bh_batch_set. */
+bh_status bh_save_snapshot(bh_ctx* ctx, const char* path);
+bh_status bh_load_snapshot(bh_ctx* ctx, const char* path);
+
 /* Host-side synthetic initial conditions (set-up time, not the per-step path): a Plummer
  * sphere of n bodies, scale radius a, total mass mtot, shifted to its centre-of-mass frame,
  * then offset by pos_offset3 / vel_offset3 (either may be null). */

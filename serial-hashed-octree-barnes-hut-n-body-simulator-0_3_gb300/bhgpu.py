@@ -38,7 +38,8 @@ EXPORTS = [
     "bh_kick_drift", "bh_kick", "bh_step", "bh_params_default", "bh_synchronize", "bh_event_record",
     "bh_event_elapsed_ms", "bh_flush_l2", "bh_host_alloc", "bh_host_free", "bh_measure_fp32_peak",
     "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step", "bh_adjoint_forward",
-    "bh_step_backward", "bh_energy_diag", "bh_autotune_walk", "bh_set_walk_variant",
+    "bh_step_backward", "bh_energy_diag", "bh_autotune_walk", "bh_set_walk_variant", "bh_plummer_device",
+    "bh_batch_plummer_device", "bh_tree_boxes", "bh_save_snapshot", "bh_load_snapshot",
 ]
 
 
@@ -152,6 +153,11 @@ def load():
         "bh_energy_diag": ([P, D, D, ctypes.POINTER(Energy), P], I),
         "bh_autotune_walk": ([P, D, D, I, ctypes.POINTER(TuneResult)], I),
         "bh_set_walk_variant": ([P, I], I),
+        "bh_plummer_device": ([P, ctypes.c_uint64, S, D, D, P, P], I),
+        "bh_batch_plummer_device": ([P, ctypes.c_uint64, P, S, D, D], I),
+        "bh_tree_boxes": ([P, S, P, P, P], I),
+        "bh_save_snapshot": ([P, ctypes.c_char_p], I),
+        "bh_load_snapshot": ([P, ctypes.c_char_p], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -327,6 +333,32 @@ class Simulation:
         r = TuneResult()
         check(self.lib.bh_autotune_walk(self.h, theta, eps, trials, ctypes.byref(r)), "bh_autotune_walk")
         return r.as_dict()
+
+    def plummer_device(self, seed, n, a=1.0, mtot=1.0, pos_offset=None, vel_offset=None):
+        """Generates a Plummer sphere on the device as the context's state (bh_plummer_device)."""
+        po = None if pos_offset is None else np.ascontiguousarray(pos_offset, np.float64)
+        vo = None if vel_offset is None else np.ascontiguousarray(vel_offset, np.float64)
+        check(self.lib.bh_plummer_device(self.h, seed, n, a, mtot, _ptr(po), _ptr(vo)), "bh_plummer_device")
+
+    def batch_plummer_device(self, seed, offsets, a=1.0, mtot=1.0):
+        """Generates an ensemble of Plummer spheres on the device (bh_batch_plummer_device)."""
+        off = np.ascontiguousarray(offsets, np.uint32)
+        check(self.lib.bh_batch_plummer_device(self.h, seed, _ptr(off), len(off) - 1, a, mtot),
+              "bh_batch_plummer_device")
+
+    def tree_boxes(self):
+        m = self.tree_size()
+        box = np.zeros((m, 4), np.float32)
+        depth = np.zeros(m, np.int32)
+        count = np.zeros(m, np.int64)
+        check(self.lib.bh_tree_boxes(self.h, m, _ptr(box), _ptr(depth), _ptr(count)), "bh_tree_boxes")
+        return box, depth, count
+
+    def save_snapshot(self, path):
+        check(self.lib.bh_save_snapshot(self.h, os.fsencode(path)), "bh_save_snapshot")
+
+    def load_snapshot(self, path):
+        check(self.lib.bh_load_snapshot(self.h, os.fsencode(path)), "bh_load_snapshot")
 
     def set_walk_variant(self, v):
         check(self.lib.bh_set_walk_variant(self.h, v), "bh_set_walk_variant")

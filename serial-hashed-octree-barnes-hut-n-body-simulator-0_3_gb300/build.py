@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libbhgpu.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["bh_api.cu", "bh_sort.cu", "bh_tree.cu", "bh_walk.cu", "bh_adjoint.cu", "bh_diag.cu", "bh_ic.cpp"]
+SOURCES = ["bh_api.cu", "bh_sort.cu", "bh_tree.cu", "bh_walk.cu", "bh_adjoint.cu", "bh_diag.cu", "bh_aux.cu", "bh_ic.cpp"]
 
 
 def _nvcc():

@@ -275,25 +275,11 @@ bh_status bh_num_bodies(const bh_ctx* c, size_t* n) {
 bh_status bh_set_state(bh_ctx* c, const float* pos_m4, const float* vel4, const float* acc4, size_t n) {
   if (!c || n > c->cap || (n > 0 && (!pos_m4 || !vel4))) return BH_ERR_INVALID_ARG;
   cudaSetDevice(c->device);
-  c->n = n;
-  c->cur = 0;
-  c->tree_valid = false;
-  c->batch = false;
-  c->batch_tree_ready = false;
-  bh::adj_invalidate(c);
-  for (auto& g : c->graph)
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  bh::reset_state(c, n);
   if (n > 0) {
     cudaMemcpyAsync(c->pos[0], pos_m4, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(c->vel[0], vel4, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream);
-    if (acc4)
-      cudaMemcpyAsync(c->acc, acc4, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream);
-    else
-      cudaMemsetAsync(c->acc, 0, sizeof(float4) * n, c->stream);
-    cudaMemsetAsync(c->body_key, 0, sizeof(uint64_t) * n, c->stream);
+    if (acc4) cudaMemcpyAsync(c->acc, acc4, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream);
   }
   return cuda_status(cudaStreamSynchronize(c->stream));
 }
@@ -785,6 +771,24 @@ bh_status bh_batch_set(bh_ctx* c, const float* pos_m4, const float* vel4, const 
   const size_t n = sys_offsets[nsys];
   if (n > c->cap) return BH_ERR_INVALID_ARG;
   BH_TRY(bh_set_state(c, pos_m4, vel4, nullptr, n));
+  return bh::batch_layout(c, sys_offsets, nsys);
+}
+
+}  // extern "C"
+
+namespace bh {
+
+bh_status check_sys_offsets(const bh_ctx* c, const uint32_t* sys_offsets, size_t nsys) {
+  if (!c || !sys_offsets || nsys == 0 || nsys > kMaxSystems || sys_offsets[0] != 0) return BH_ERR_INVALID_ARG;
+  for (size_t s = 0; s < nsys; ++s)
+    if (sys_offsets[s + 1] <= sys_offsets[s]) return BH_ERR_INVALID_ARG;  // every system has a body
+  return sys_offsets[nsys] > c->cap ? BH_ERR_INVALID_ARG : BH_OK;
+}
+
+// Ensemble layout over the bodies already in the state: system ids per slot, walk groups that
+// never straddle systems, per-system geometry storage.
+bh_status batch_layout(bh_ctx* c, const uint32_t* sys_offsets, size_t nsys) {
+  const size_t n = sys_offsets[nsys];
   cudaSetDevice(c->device);
   destroy_graphs(c);
   if (c->sys_cap < nsys) {
@@ -814,6 +818,27 @@ bh_status bh_batch_set(bh_ctx* c, const float* pos_m4, const float* vel4, const 
   c->batch = true;
   return BH_OK;
 }
+
+// A new state of n bodies in slot order 0..n-1: every derived structure (tree, ensemble layout,
+// captured graphs, recorded trajectory) is dropped; accelerations and Morton keys are zeroed. The
+// caller fills pos[0] / vel[0].
+void reset_state(bh_ctx* c, size_t n) {
+  c->n = n;
+  c->cur = 0;
+  c->tree_valid = false;
+  c->batch = false;
+  c->batch_tree_ready = false;
+  adj_invalidate(c);
+  destroy_graphs(c);
+  if (n > 0) {
+    cudaMemsetAsync(c->acc, 0, sizeof(float4) * n, c->stream);
+    cudaMemsetAsync(c->body_key, 0, sizeof(uint64_t) * n, c->stream);
+  }
+}
+
+}  // namespace bh
+
+extern "C" {
 
 bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
   if (!c || !prm || nsteps < 0 || !c->batch || prm->leaf_capacity < 1 || !(prm->theta >= 0) || !(prm->eps >= 0) ||

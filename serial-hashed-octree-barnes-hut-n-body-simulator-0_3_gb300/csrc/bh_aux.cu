@@ -1,0 +1,312 @@
+// Around the step: initial conditions generated on the device, snapshot files, and the node
+// boxes of the current tree for visualisation. None of these has a counterpart on the
+// reference's hot path: the reference builds its bodies on the host
+// (SetupSolarSystem / PhysicsHelpers, src/PhysicsHelpers.hpp:268-683) and draws node boxes with
+// openFrameworks (visualizeTree, src/HashedOctree.cpp:939-974), which has no headless form.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "bh_internal.cuh"
+
+namespace bh {
+namespace {
+
+constexpr int kThreads = 256;
+
+// ---------------------------------------------------------------------------------------
+// Plummer spheres on the device
+// ---------------------------------------------------------------------------------------
+
+// Counter-based uniforms: splitmix64's output mix applied to (seed, body, draw), so every body
+// draws its own numbers independently of the others and of the launch shape.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double uniform(uint64_t seed, uint64_t body, uint32_t draw) {
+  const uint64_t z = mix64(mix64(seed + 0x9e3779b97f4a7c15ull * (body + 1)) ^ (0x632be59bd9b4e019ull * (draw + 1)));
+  return ((double)(z >> 11) + 0.5) * 0x1p-53;  // in (0, 1)
+}
+
+struct Sample {
+  double x[3], v[3];
+};
+
+// One body of a Plummer sphere with G = M = a = 1 (the recipe of the host generator bh_plummer):
+// r = 1 / sqrt(U^(-2/3) - 1) with r > 10 rejected; speed q sqrt(2) (1 + r^2)^(-1/4) with q drawn
+// by rejection from q^2 (1 - q^2)^(7/2) under the bound 0.1; isotropic directions. Each
+// rejection loop has 64 rounds (the probabilities of exhausting them are below 1e-100 and
+// 1e-12); an exhausted loop keeps its last draw.
+__device__ Sample plummer_body(uint64_t seed, uint64_t j) {
+  uint32_t draw = 0;
+  double r = 0;
+  for (int t = 0; t < 64; ++t) {
+    const double u = uniform(seed, j, draw++);
+    r = 1.0 / sqrt(pow(u, -2.0 / 3.0) - 1.0);
+    if (r <= 10.0) break;
+  }
+  double q = 0;
+  for (int t = 0; t < 64; ++t) {
+    q = uniform(seed, j, draw++);
+    const double g = 0.1 * uniform(seed, j, draw++);
+    if (g <= q * q * pow(1.0 - q * q, 3.5)) break;
+  }
+  const double speed = q * sqrt(2.0) * pow(1.0 + r * r, -0.25);
+  Sample s;
+  double* out[2] = {s.x, s.v};
+  const double mag[2] = {r, speed};
+  for (int k = 0; k < 2; ++k) {
+    const double ct = 2.0 * uniform(seed, j, draw++) - 1.0;
+    const double ph = 6.283185307179586 * uniform(seed, j, draw++);
+    const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+    out[k][0] = mag[k] * st * cos(ph);
+    out[k][1] = mag[k] * st * sin(ph);
+    out[k][2] = mag[k] * ct;
+  }
+  return s;
+}
+
+// System of slot i: a binary search of the system offsets (one system when off is null).
+__device__ __forceinline__ int system_of(const uint32_t* __restrict__ off, int nsys, uint32_t i) {
+  if (!off) return 0;
+  int lo = 0, hi = nsys - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// pass 0: per-system sums of positions and velocities (FP64; a warp whose lanes share a system
+// adds once); pass 1: regenerate, subtract the system's mean, scale, write the state.
+__global__ __launch_bounds__(kThreads) void k_plummer(int pass, int n, const uint32_t* __restrict__ off, int nsys,
+                                                      uint64_t seed, double a, double mtot,
+                                                      const double* __restrict__ offs6, double* __restrict__ sums,
+                                                      float4* __restrict__ pos, float4* __restrict__ vel) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  const bool ok = i < n;
+  const int s = ok ? system_of(off, nsys, (uint32_t)i) : -1;
+  const uint32_t b0 = off ? off[ok ? s : 0] : 0u;
+  const uint32_t nb = off ? off[(ok ? s : 0) + 1] - b0 : (uint32_t)n;
+  Sample smp{};
+  if (ok) smp = plummer_body(seed + (uint64_t)s, (uint64_t)i - b0);
+  if (pass == 0) {
+    const int lead = __shfl_sync(0xffffffffu, s, 0);
+    const bool uniform_sys = __all_sync(0xffffffffu, s == lead);
+    double v[6] = {smp.x[0], smp.x[1], smp.x[2], smp.v[0], smp.v[1], smp.v[2]};
+    if (uniform_sys) {
+#pragma unroll
+      for (int k = 0; k < 6; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+      if ((threadIdx.x & 31) == 0 && lead >= 0)
+        for (int k = 0; k < 6; ++k) atomicAdd(sums + 6 * lead + k, v[k]);
+    } else if (ok) {
+      for (int k = 0; k < 6; ++k) atomicAdd(sums + 6 * s + k, v[k]);
+    }
+    return;
+  }
+  if (!ok) return;
+  const double inv = 1.0 / (double)nb, vs = sqrt(mtot / a);
+  double x[3], u[3];
+  for (int k = 0; k < 3; ++k) {
+    x[k] = a * (smp.x[k] - sums[6 * s + k] * inv) + (offs6 ? offs6[k] : 0.0);
+    u[k] = vs * (smp.v[k] - sums[6 * s + 3 + k] * inv) + (offs6 ? offs6[3 + k] : 0.0);
+  }
+  pos[i] = make_float4((float)x[0], (float)x[1], (float)x[2], (float)(mtot / (double)nb));
+  vel[i] = make_float4((float)u[0], (float)u[1], (float)u[2], 0.f);
+}
+
+bh_status generate(bh_ctx* c, uint64_t seed, int n, const uint32_t* off_dev, int nsys, double a, double mtot,
+                   const double* offs6_host) {
+  double* sums = nullptr;
+  double* offs6 = nullptr;
+  BH_TRY(dalloc(&sums, (size_t)6 * nsys));
+  if (offs6_host && dalloc(&offs6, 6) != BH_OK) {
+    dfree(sums);
+    return BH_ERR_OOM;
+  }
+  cudaMemsetAsync(sums, 0, sizeof(double) * 6 * nsys, c->stream);
+  if (offs6) cudaMemcpyAsync(offs6, offs6_host, sizeof(double) * 6, cudaMemcpyHostToDevice, c->stream);
+  const int grid = (n + kThreads - 1) / kThreads;
+  c->launches += 2;
+  for (int pass = 0; pass < 2; ++pass)
+    k_plummer<<<grid, kThreads, 0, c->stream>>>(pass, n, off_dev, nsys, seed, a, mtot, offs6, sums, c->pos[0],
+                                                 c->vel[0]);
+  bh_status s = last_launch();
+  if (s == BH_OK) s = cuda_status(cudaStreamSynchronize(c->stream));
+  dfree(sums);
+  dfree(offs6);
+  return s;
+}
+
+// ---------------------------------------------------------------------------------------
+// node boxes
+// ---------------------------------------------------------------------------------------
+
+// Centre and edge of every node from its key: the root cube, then per level the reference's
+// child-bounds recurrence (size' = size / 2, centre' = centre + (+-0.5) size', one FP64 rounding
+// per axis and level, src/HashedNode.cpp:48-70).
+__global__ __launch_bounds__(kThreads) void k_node_boxes(const uint64_t* __restrict__ nkey,
+                                                         const int2* __restrict__ nrange, int m, double c0,
+                                                         double c1, double c2, double edge,
+                                                         float4* __restrict__ box, int* __restrict__ depth,
+                                                         long long* __restrict__ count) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= m) return;
+  const uint64_t key = nkey[i];
+  const int d = (63 - __clzll((long long)key)) / 3;
+  double c[3] = {c0, c1, c2}, s = edge;
+  for (int l = d - 1; l >= 0; --l) {
+    const int oct = (int)((key >> (3 * l)) & 7u);
+    s = __dmul_rn(s, 0.5);
+    for (int a = 0; a < 3; ++a) {
+      const double dir = ((oct >> (2 - a)) & 1) ? 0.5 : -0.5;
+      c[a] = __dadd_rn(c[a], __dmul_rn(dir, s));
+    }
+  }
+  if (box) box[i] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)s);
+  if (depth) depth[i] = d;
+  if (count) count[i] = nrange[i].y;
+}
+
+// Snapshot file: a 64-byte header, then pos_m (float4 x n), vel (float4 x n), acc (float4 x n)
+// and, for an ensemble, the system offsets (u32 x (nsys + 1)). Little-endian, as both host
+// architectures that run the library are.
+struct SnapHeader {
+  char magic[8];      // "BHGPUSNP"
+  uint32_t version;   // 1
+  uint32_t flags;     // bit 0: ensemble
+  uint64_t n;
+  uint64_t nsys;
+  uint64_t reserved[4];
+};
+static_assert(sizeof(SnapHeader) == 64, "snapshot header is 64 bytes");
+
+}  // namespace
+}  // namespace bh
+
+using namespace bh;
+
+extern "C" {
+
+bh_status bh_plummer_device(bh_ctx* c, uint64_t seed, size_t n, double a, double mtot, const double* pos_offset3,
+                            const double* vel_offset3) {
+  if (!c || n == 0 || n > c->cap || !(a > 0) || !(mtot > 0)) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  reset_state(c, n);
+  double offs[6] = {0, 0, 0, 0, 0, 0};
+  for (int k = 0; k < 3; ++k) {
+    if (pos_offset3) offs[k] = pos_offset3[k];
+    if (vel_offset3) offs[3 + k] = vel_offset3[k];
+  }
+  return generate(c, seed, (int)n, nullptr, 1, a, mtot, (pos_offset3 || vel_offset3) ? offs : nullptr);
+}
+
+bh_status bh_batch_plummer_device(bh_ctx* c, uint64_t seed, const uint32_t* sys_offsets, size_t nsys, double a,
+                                  double mtot) {
+  BH_TRY(check_sys_offsets(c, sys_offsets, nsys));
+  if (!(a > 0) || !(mtot > 0)) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  const size_t n = sys_offsets[nsys];
+  reset_state(c, n);
+  BH_TRY(batch_layout(c, sys_offsets, nsys));
+  return generate(c, seed, (int)n, c->sys_off, (int)nsys, a, mtot, nullptr);
+}
+
+bh_status bh_tree_boxes(bh_ctx* c, size_t cap, float* center_edge4, int32_t* depth, int64_t* count) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  if (!c->tree_valid) return BH_ERR_NO_TREE;
+  cudaSetDevice(c->device);
+  const size_t m = c->n ? (size_t)c->h_level_bounds[kLevels] : 0;
+  if (cap < m) return BH_ERR_INVALID_ARG;
+  if (m == 0) return BH_OK;
+  float4* box = nullptr;
+  int* dep = nullptr;
+  long long* cnt = nullptr;
+  bh_status s = BH_OK;
+  if (center_edge4 && s == BH_OK) s = dalloc(&box, m);
+  if (depth && s == BH_OK) s = dalloc(&dep, m);
+  if (count && s == BH_OK) s = dalloc(&cnt, m);
+  if (s == BH_OK) {
+    c->launches += 1;
+    k_node_boxes<<<(int)((m + kThreads - 1) / kThreads), kThreads, 0, c->stream>>>(
+        c->nkey, c->nrange, (int)m, c->tree_center[0], c->tree_center[1], c->tree_center[2], c->tree_edge, box,
+        dep, cnt);
+    s = last_launch();
+  }
+  if (s == BH_OK && box) cudaMemcpyAsync(center_edge4, box, sizeof(float4) * m, cudaMemcpyDeviceToHost, c->stream);
+  if (s == BH_OK && dep) cudaMemcpyAsync(depth, dep, sizeof(int) * m, cudaMemcpyDeviceToHost, c->stream);
+  if (s == BH_OK && cnt) cudaMemcpyAsync(count, cnt, sizeof(long long) * m, cudaMemcpyDeviceToHost, c->stream);
+  if (s == BH_OK) s = cuda_status(cudaStreamSynchronize(c->stream));
+  dfree(box);
+  dfree(dep);
+  dfree(cnt);
+  return s;
+}
+
+bh_status bh_save_snapshot(bh_ctx* c, const char* path) {
+  if (!c || !path) return BH_ERR_INVALID_ARG;
+  const size_t n = c->n;
+  std::vector<float> p(4 * n), v(4 * n), acc(4 * n);
+  BH_TRY(bh_get_bodies(c, p.data(), v.data(), acc.data()));
+  std::vector<uint32_t> off;
+  if (c->batch) {
+    off.resize((size_t)c->nsys + 1);
+    cudaMemcpy(off.data(), c->sys_off, sizeof(uint32_t) * off.size(), cudaMemcpyDeviceToHost);
+    BH_TRY(last_launch());
+  }
+  SnapHeader h{};
+  std::memcpy(h.magic, "BHGPUSNP", 8);
+  h.version = 1;
+  h.flags = c->batch ? 1u : 0u;
+  h.n = n;
+  h.nsys = c->batch ? (uint64_t)c->nsys : 0;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return BH_ERR_INVALID_ARG;
+  bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
+  if (n) {
+    ok = ok && std::fwrite(p.data(), sizeof(float), p.size(), f) == p.size();
+    ok = ok && std::fwrite(v.data(), sizeof(float), v.size(), f) == v.size();
+    ok = ok && std::fwrite(acc.data(), sizeof(float), acc.size(), f) == acc.size();
+  }
+  if (!off.empty()) ok = ok && std::fwrite(off.data(), sizeof(uint32_t), off.size(), f) == off.size();
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? BH_OK : BH_ERR_INVALID_ARG;
+}
+
+bh_status bh_load_snapshot(bh_ctx* c, const char* path) {
+  if (!c || !path) return BH_ERR_INVALID_ARG;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return BH_ERR_INVALID_ARG;
+  SnapHeader h{};
+  bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, "BHGPUSNP", 8) == 0 && h.version == 1 &&
+            h.n <= c->cap && (!(h.flags & 1u) || (h.nsys >= 1 && h.nsys <= 65535));
+  std::vector<float> p, v, acc;
+  std::vector<uint32_t> off;
+  if (ok) {
+    p.resize(4 * h.n);
+    v.resize(4 * h.n);
+    acc.resize(4 * h.n);
+    ok = std::fread(p.data(), sizeof(float), p.size(), f) == p.size() &&
+         std::fread(v.data(), sizeof(float), v.size(), f) == v.size() &&
+         std::fread(acc.data(), sizeof(float), acc.size(), f) == acc.size();
+  }
+  if (ok && (h.flags & 1u)) {
+    off.resize(h.nsys + 1);
+    ok = std::fread(off.data(), sizeof(uint32_t), off.size(), f) == off.size() && off[h.nsys] == h.n;
+  }
+  std::fclose(f);
+  if (!ok) return BH_ERR_INVALID_ARG;
+  if (h.flags & 1u) BH_TRY(check_sys_offsets(c, off.data(), h.nsys));
+  BH_TRY(bh_set_state(c, p.data(), v.data(), acc.data(), h.n));
+  if (h.flags & 1u) return batch_layout(c, off.data(), h.nsys);
+  return BH_OK;
+}
+
+}  // extern "C"

@@ -257,5 +257,10 @@ void launch_walk_variant(bh_ctx* c, int v, int n, float theta, float eps, float4
 void adj_release(bh_ctx* c);
 // Marks the recorded trajectory stale (new bodies were uploaded).
 void adj_invalidate(bh_ctx* c);
+// New state of n bodies (bh_api.cu): derived structures dropped, accelerations and keys zeroed.
+void reset_state(bh_ctx* c, size_t n);
+// Ensemble layout over the bodies already in the state (bh_api.cu).
+bh_status check_sys_offsets(const bh_ctx* c, const uint32_t* sys_offsets, size_t nsys);
+bh_status batch_layout(bh_ctx* c, const uint32_t* sys_offsets, size_t nsys);
 
 }  // namespace bh
