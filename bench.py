@@ -185,7 +185,7 @@ def ncu_traffic():
     return None
 
 
-def accuracy_vs_direct(w, pm, acc_by_theta, orc, nthreads, ntarget=1024):
+def accuracy_vs_direct(w, pm, acc_by_theta, orc, nthreads, ntarget=1024, tree=None):
     """Median / p99 relative error of the step-0 accelerations against the FP64 direct sum on a
     seeded subsample (the benchmark spec's <= 1e-3 gate), for the workload's theta and the others
     of the at-scale sweep."""
@@ -201,8 +201,16 @@ def accuracy_vs_direct(w, pm, acc_by_theta, orc, nthreads, ntarget=1024):
         err = relerr(acc[tgt], d)
         out[f"{theta:g}"] = {"median": float(np.median(err)), "p99": float(np.percentile(err, 99))}
     main = out[f"{w['theta']:g}"]
-    return {"median_rel_err_vs_direct_fp64": main["median"], "p99": main["p99"], "targets": int(len(tgt)),
-            "by_theta": out}
+    res = {"median_rel_err_vs_direct_fp64": main["median"], "p99": main["p99"], "targets": int(len(tgt)),
+           "by_theta": out}
+    if tree is not None:
+        # the reference's tree walk (the oracle restatement, FP64) at the same theta, softening,
+        # leaf size and root cube, on the same targets
+        c, edge = tree
+        ref, _, _ = orc.force(pos, mass, c, edge, w["leaf"], 1, w["theta"], w["eps"], targets=tgt, nthreads=nthreads)
+        err = relerr(acc_by_theta[w["theta"]][tgt], ref)
+        res["vs_reference_walk"] = {"median": float(np.median(err)), "p99": float(np.percentile(err, 99))}
+    return res
 
 
 def cpu_sample(bh, w, pm, nthreads, walk_sample):
@@ -300,7 +308,8 @@ def run_ours(args, w, dist):
         c, size = sim.bounds()
         sim.build(c, size * w["edge"], w["leaf"], bh.BH_MULTIPOLE_QUADRUPOLE)
         accs = {th: sim.force(th, w["eps"]) for th in sorted({0.3, 0.5, 0.7, w["theta"]})}
-        accuracy = accuracy_vs_direct(w, pm, accs, Restatement(), os.cpu_count() or 1)
+        accuracy = accuracy_vs_direct(w, pm, accs, Restatement(), os.cpu_count() or 1,
+                                      tree=(c, size * w["edge"]))
         sim.set_bodies(pm, vel)
 
     fp32_peak = sim.fp32_peak_tflops()
@@ -430,28 +439,8 @@ def run_ours(args, w, dist):
 
 
 ENSEMBLE = dict(nsys=4096, nmin=256, nmax=65536, theta=0.6, eps=0.01, leaf=8, dt=1e-3, edge=2.0, seed=1000,
-                desc="4096 Plummer systems (seed 1000 + s), N_s = round(exp(U ln 256 + ln 256)) in [256, 65536], "
-                     "M = a = 1 each, theta=0.6, eps=0.01, leaf 8, dt=1e-3, quadrupole, edge 2S")
-
-
-def make_ensemble(bh, e):
-    import concurrent.futures
-
-    rng = np.random.default_rng(e["seed"])
-    u = rng.uniform(0.0, 1.0, e["nsys"])
-    sizes = np.round(np.exp(u * np.log(e["nmax"] / e["nmin"]) + np.log(e["nmin"]))).astype(np.int64)
-    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint32)
-    pos = np.zeros((int(off[-1]), 4), np.float32)
-    vel = np.zeros_like(pos)
-
-    def one(s):
-        p, v = bh.plummer(e["seed"] + s, int(sizes[s]))
-        pos[off[s]:off[s + 1]] = p
-        vel[off[s]:off[s + 1]] = v
-
-    with concurrent.futures.ThreadPoolExecutor(os.cpu_count() or 4) as ex:
-        list(ex.map(one, range(e["nsys"])))
-    return pos, vel, off
+                desc="4096 Plummer systems (device generator, seed 1000 + s), N_s = round(exp(U ln 256 + ln 256)) "
+                     "in [256, 65536], M = a = 1 each, theta=0.6, eps=0.01, leaf 8, dt=1e-3, quadrupole, edge 2S")
 
 
 def run_ensemble(args, dist):
@@ -463,12 +452,17 @@ def run_ensemble(args, dist):
     bh = __graft_entry__.package()
     bh.load()
     e = ENSEMBLE
-    pos, vel, off = make_ensemble(bh, e)
+    rng = np.random.default_rng(e["seed"])
+    u = rng.uniform(0.0, 1.0, e["nsys"])
+    sizes = np.round(np.exp(u * np.log(e["nmax"] / e["nmin"]) + np.log(e["nmin"]))).astype(np.int64)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint32)
     n = int(off[-1])
     prm = bh.default_params(theta=e["theta"], eps=e["eps"], dt=e["dt"], leaf_capacity=e["leaf"],
                             multipole=bh.BH_MULTIPOLE_QUADRUPOLE, edge_factor=e["edge"], acc_follows_body=1)
     sim = bh.Simulation(n)
-    sim.batch_set(pos, vel, off)
+    # the ensemble's initial conditions come from the device generator (system s: seed + s)
+    sim.batch_plummer_device(e["seed"], off)
+    pos, vel, _ = sim.get_bodies()
     fp32_peak = sim.fp32_peak_tflops()
     sim.batch_step(prm, 1, stats=False)
     tune = sim.autotune(e["theta"], e["eps"], trials=2)  # walk launch shape for this ensemble

@@ -861,7 +861,10 @@ bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* s
       if (!c->graph[par]) {
         cudaGraph_t g = nullptr;
         BH_TRY(cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)));
+        const uint64_t l0 = c->launches;
         enqueue_batch_step(c, *prm);
+        c->graph_kernels[par] = c->launches - l0;  // counted when the graph runs, not when captured
+        c->launches = l0;
         cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
         if (ce != cudaSuccess || !g) return cuda_status(ce == cudaSuccess ? cudaErrorUnknown : ce);
         ce = cudaGraphInstantiate(&c->graph[par], g, 0);
@@ -873,6 +876,7 @@ bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* s
       }
       if (st) cudaEventRecord(c->stage_ev[0], c->stream);
       BH_TRY(cuda_status(cudaGraphLaunch(c->graph[par], c->stream)));
+      c->launches += c->graph_kernels[par];
       if (st) cudaEventRecord(c->stage_ev[1], c->stream);
       BH_TRY(sync_and_check(c, &e));
       if (e & bh::kErrNodes) {  // arena too small: grow it, re-capture, redo the step
