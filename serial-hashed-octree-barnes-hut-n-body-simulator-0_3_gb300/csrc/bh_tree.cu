@@ -408,6 +408,39 @@ __device__ __forceinline__ int ld_relaxed_i(const int* p) {
 constexpr uint32_t kLbAgg = 1u << 30, kLbPrefix = 2u << 30, kLbMask = (1u << 30) - 1;
 constexpr int kLbSpin = 1 << 22;
 
+// K independent binary searches in the sorted child digits of one node: search j finds, inside
+// [bnd[2Hj], bnd[2H(j+1)]), the first index whose digit is >= 2Hj + H, and stores it there.
+template <int K, int H>
+__device__ __forceinline__ void split_search(const uint64_t* __restrict__ tkey, int shift, int (&bnd)[9]) {
+  int a[K], b[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    a[j] = bnd[2 * H * j];
+    b[j] = bnd[2 * H * (j + 1)];
+  }
+  for (;;) {
+    bool any = false;
+#pragma unroll
+    for (int j = 0; j < K; ++j) any |= a[j] < b[j];
+    if (!any) break;
+    int dig[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j)  // loads first, so the K searches wait on the memory together
+      dig[j] = a[j] < b[j] ? (int)((tkey[(a[j] + b[j]) >> 1] >> shift) & 7ull) : 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (a[j] >= b[j]) continue;
+      const int m = (a[j] + b[j]) >> 1;
+      if (dig[j] < 2 * H * j + H)
+        a[j] = m + 1;
+      else
+        b[j] = m;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < K; ++j) bnd[2 * H * j + H] = a[j];
+}
+
 __global__ __launch_bounds__(kThreads) void k_level(int d, const uint64_t* __restrict__ tkey, int leaf_cap,
                                                     uint64_t* __restrict__ nkey, int2* __restrict__ nrange,
                                                     WalkNode* __restrict__ wn, uint8_t* __restrict__ childbyte,
@@ -447,20 +480,14 @@ __global__ __launch_bounds__(kThreads) void k_level(int d, const uint64_t* __res
       r = nrange[node];
       internal = r.y > leaf_cap && d < kMaxDepth;
       if (internal) {
+        // the first index with child digit >= v, for v = 4, then 2 and 6, then 1, 3, 5, 7: each
+        // round searches inside the intervals the previous round split off, and its searches are
+        // independent, so their loads overlap (three dependent search depths instead of seven)
         bnd[0] = r.x;
         bnd[8] = r.x + r.y;
-        for (int v = 1; v < 8; ++v) {
-          int a = bnd[v - 1], b = bnd[8];  // first index with digit >= v lies in [a, b]
-          while (a < b) {
-            int m = (a + b) >> 1;
-            int dig = (int)((tkey[m] >> shift) & 7ull);
-            if (dig < v)
-              a = m + 1;
-            else
-              b = m;
-          }
-          bnd[v] = a;
-        }
+        split_search<1, 4>(tkey, shift, bnd);
+        split_search<2, 2>(tkey, shift, bnd);
+        split_search<4, 1>(tkey, shift, bnd);
         for (int v = 0; v < 8; ++v)
           if (bnd[v + 1] > bnd[v]) {
             ++nc;
@@ -600,6 +627,8 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int
         min_rank = tslot[link.z];
         single = true;
       } else {
+        // unrolled so that several members' loads are in flight before the dependent sums
+#pragma unroll 4
         for (int b = link.z; b < link.z + link.w; ++b) {
           const float4 p = tpos[b];
           mass = ff_add(mass, {p.w, 0.f});
@@ -610,6 +639,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int
         }
         if (mass.hi != 0.f)
           for (int a = 0; a < 3; ++a) com[a] = ff_div(com[a], mass);
+#pragma unroll 4
         for (int b = link.z; b < link.z + link.w; ++b) {
           const float4 p = tpos[b];
           quad_add(q, p.w, (p.x - com[0].hi) - com[0].lo, (p.y - com[1].hi) - com[1].lo,
