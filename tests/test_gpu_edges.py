@@ -1,0 +1,85 @@
+"""Edge cases across the entry points: empty states, one or two bodies, ensembles of tiny
+systems, and the differentiable path on the smallest inputs."""
+import numpy as np
+import pytest
+
+from oracle.oracle import direct_adjoint, relerr
+
+pytestmark = pytest.mark.gpu
+
+
+def test_empty_state(bh, tmp_path):
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1)
+    with bh.Simulation(16) as sim:
+        sim.set_bodies(np.zeros((0, 4), np.float32), np.zeros((0, 4), np.float32))
+        st = sim.step(prm, 3)
+        assert st.steps == 0
+        p, v, a = sim.get_bodies()
+        assert p.shape == (0, 4)
+        path = str(tmp_path / "empty.bhsnap")
+        sim.save_snapshot(path)
+        sim.load_snapshot(path)
+        assert sim.n == 0
+
+
+@pytest.mark.parametrize("n", [1, 2])
+def test_one_and_two_bodies(bh, n):
+    pm = np.array([[0.1, -0.2, 0.3, 0.5], [-0.4, 0.25, 0.0, 0.25]], np.float32)[:n]
+    vel = np.zeros((n, 4), np.float32)
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=1, multipole=1, edge_factor=2.0)
+    with bh.Simulation(4) as sim:
+        sim.set_bodies(pm, vel)
+        sim.step(prm, 5)
+        p, v, acc = sim.get_bodies()
+        assert np.all(np.isfinite(p)) and np.all(np.isfinite(acc))
+        e = sim.energy(0.5, 0.01)
+        box, depth, count = sim.tree_boxes()
+        assert count[0] == n and depth[0] == 0
+    if n == 1:
+        assert np.all(acc[:, :3] == 0) and e["potential"] == 0.0
+    else:
+        # equal and opposite momenta change: sum m a = 0
+        assert np.allclose((p[:, 3:4] * acc[:, :3]).sum(0), 0, atol=1e-6)
+        assert e["potential"] < 0
+
+
+def test_ensemble_of_tiny_systems(bh):
+    sizes = [1, 2, 3, 31, 32, 33, 1, 64, 65, 2]
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint32)
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=1, multipole=1, edge_factor=2.0)
+    pos, vel = [], []
+    for s, k in enumerate(sizes):
+        p, v = bh.plummer(500 + s, k)
+        v[:, 3] = np.arange(k, dtype=np.float32)
+        pos.append(p)
+        vel.append(v)
+    pm, vv = np.concatenate(pos), np.concatenate(vel)
+    with bh.Simulation(len(pm)) as sim:
+        sim.batch_set(pm, vv, off)
+        sim.batch_step(prm, 3)
+        bp, bv, ba = sim.get_bodies()
+    with bh.Simulation(max(sizes)) as one:
+        for s in range(len(sizes)):
+            a, b = off[s], off[s + 1]
+            one.set_bodies(pm[a:b], vv[a:b])
+            one.step(prm, 3)
+            p, v, acc = one.get_bodies()
+            assert np.array_equal(bv[a:b, 3], v[:, 3])
+            assert np.allclose(bp[a:b], p, rtol=0, atol=1e-6)
+            if sizes[s] > 1:
+                assert float(relerr(ba[a:b], acc).max()) < 1e-5
+
+
+def test_adjoint_two_bodies_matches_direct_adjoint(bh, orc):
+    pm = np.array([[0.1, -0.2, 0.3, 0.5], [-0.4, 0.25, 0.0, 0.25]], np.float32)
+    vel = np.array([[0.0, 0.1, 0.0, 0.0], [0.05, -0.2, 0.0, 0.0]], np.float32)
+    prm = bh.default_params(theta=0.5, eps=0.05, dt=1e-2, leaf_capacity=1, multipole=1, edge_factor=2.0)
+    dl = np.array([[1.0, -0.5, 0.25], [0.3, 0.2, -0.1]], np.float32)
+    with bh.Simulation(2) as sim:
+        sim.set_bodies(pm, vel)
+        sim.adjoint_forward(prm, 30, 7)
+        gx, gv, gm = sim.step_backward(dl, None)
+    _, _, rx, rv, rm = direct_adjoint(orc, pm[:, :3], vel[:, :3], pm[:, 3], 1e-2, 0.05, 30, dl.astype(np.float64))
+    assert np.allclose(gx[:, :3], rx, rtol=1e-4, atol=1e-6)
+    assert np.allclose(gv[:, :3], rv, rtol=1e-4, atol=1e-6)
+    assert np.allclose(gm, rm, rtol=1e-4, atol=1e-6)
