@@ -41,6 +41,10 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "plummer-4m": dict(n=1 << 22, theta=0.5, eps=0.005, leaf=16, dt=5e-4, edge=2.0, kind="plummer", seed=0,
                        desc="Plummer sphere N=2^22, theta=0.5, eps=0.005, leaf 16, dt=5e-4, quadrupole, edge 2S"),
+    "plummer-4m-theta0.3": dict(n=1 << 22, theta=0.3, eps=0.005, leaf=16, dt=5e-4, edge=2.0, kind="plummer", seed=0,
+                                desc="Plummer sphere N=2^22, theta=0.3, eps=0.005, leaf 16, dt=5e-4, quadrupole, edge 2S"),
+    "plummer-4m-theta0.7": dict(n=1 << 22, theta=0.7, eps=0.005, leaf=16, dt=5e-4, edge=2.0, kind="plummer", seed=0,
+                                desc="Plummer sphere N=2^22, theta=0.7, eps=0.005, leaf 16, dt=5e-4, quadrupole, edge 2S"),
     "plummer-16k": dict(n=16384, theta=0.5, eps=0.01, leaf=1, dt=1e-3, edge=2.0, kind="plummer", seed=0,
                         desc="Plummer sphere N=16384, theta=0.5, eps=0.01, leaf 1, dt=1e-3, quadrupole, edge 2S"),
     # profiling sizes of the headline recipe (small enough for full ncu captures / larger than L2)
