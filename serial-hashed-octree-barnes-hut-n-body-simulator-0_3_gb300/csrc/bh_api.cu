@@ -110,7 +110,10 @@ void record(bh_ctx* c, bh_stats* st, int k) {
 
 float elapsed(bh_ctx* c, int a, int b) {
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, c->stage_ev[a], c->stage_ev[b]);
+  if (cudaEventElapsedTime(&ms, c->stage_ev[a], c->stage_ev[b]) != cudaSuccess) {
+    cudaGetLastError();  // a timing that cannot be read is reported as 0, not as a launch error
+    ms = 0.f;
+  }
   return ms;
 }
 
@@ -120,6 +123,8 @@ using namespace bh;
 
 namespace {
 constexpr size_t kMaxBodies = (1u << 30) - 1;  // sort look-back words hold 30-bit counts
+void destroy_graphs(bh_ctx* c);
+bool same_params(const bh_params& a, const bh_params& b);
 }  // namespace
 
 extern "C" {
@@ -566,31 +571,64 @@ bh_status bh_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
   BH_TRY(ensure_nodes(c, initial_node_cap(c->n)));
   const float dt = (float)prm->dt;
   const uint64_t launches0 = c->launches;
+  // One step as a CUDA graph per state parity (the ping-pong buffers alternate), captured on
+  // first use and replayed: the step's ~70 launches cost one graph launch. Stage events are
+  // recorded inside the graph as external event-record nodes (a plain record during capture
+  // would only order the capture, not record the event).
+  auto mark = [&](int k) { cudaEventRecordWithFlags(c->stage_ev[k], c->stream, cudaEventRecordExternal); };
+  auto enqueue_step = [&]() {
+    const int nx = 1 - c->cur;
+    clear_device_flags(c);
+    mark(0);
+    bh::launch_bounds(c, c->pos[c->cur], n, prm->edge_factor);
+    mark(1);
+    bh::launch_morton(c, c->pos[c->cur], n, c->keys[0], c->vals[0]);
+    mark(2);
+    uint64_t* ko;
+    uint32_t* perm;
+    bh::radix_sort_pairs(c, c->keys[0], c->vals[0], c->keys[1], c->vals[1], n, c->stream, &ko, &perm);
+    mark(3);
+    bh::launch_gather_kd_treekey(c, perm, n, c->pos[c->cur], c->vel[c->cur], c->acc, prm->acc_follows_body, dt,
+                                 c->pos[nx], c->vel[nx], c->tkey, c->tslot);
+    mark(4);
+    enqueue_tree(c, c->pos[nx], n, prm->leaf_capacity, prm->multipole, true);
+    mark(5);
+    bh::launch_build(c, n, prm->leaf_capacity);
+    mark(6);
+    bh::launch_upsweep(c, n, prm->leaf_capacity, prm->multipole);
+    mark(7);
+    bh::launch_walk(c, n, (float)prm->theta, (float)prm->eps, prm->multipole, c->acc, c->vel[nx], 0.5f * dt);
+    mark(8);
+  };
+  if (!same_params(c->graph_params, *prm)) destroy_graphs(c);
+  c->graph_params = *prm;
   for (int s = 0; s < nsteps; ++s) {
     uint32_t e = 0;
     for (;;) {
-      const int nx = 1 - c->cur;
-      clear_device_flags(c);
-      record(c, st, 0);
-      bh::launch_bounds(c, c->pos[c->cur], n, prm->edge_factor);
-      record(c, st, 1);
-      bh::launch_morton(c, c->pos[c->cur], n, c->keys[0], c->vals[0]);
-      record(c, st, 2);
-      uint64_t* ko;
-      uint32_t* perm;
-      bh::radix_sort_pairs(c, c->keys[0], c->vals[0], c->keys[1], c->vals[1], n, c->stream, &ko, &perm);
-      record(c, st, 3);
-      bh::launch_gather_kd_treekey(c, perm, n, c->pos[c->cur], c->vel[c->cur], c->acc, prm->acc_follows_body, dt,
-                                   c->pos[nx], c->vel[nx], c->tkey, c->tslot);
-      record(c, st, 4);
-      enqueue_tree(c, c->pos[nx], n, prm->leaf_capacity, prm->multipole, true);
-      record(c, st, 5);
-      bh::launch_build(c, n, prm->leaf_capacity);
-      record(c, st, 6);
-      bh::launch_upsweep(c, n, prm->leaf_capacity, prm->multipole);
-      record(c, st, 7);
-      bh::launch_walk(c, n, (float)prm->theta, (float)prm->eps, prm->multipole, c->acc, c->vel[nx], 0.5f * dt);
-      record(c, st, 8);
+      const int par = c->cur;
+      if (c->graph[par] && c->graph_keys0[par] != c->keys[0]) {  // the key buffers were swapped since
+        cudaGraphExecDestroy(c->graph[par]);
+        c->graph[par] = nullptr;
+      }
+      if (!c->graph[par]) {
+        cudaGraph_t g = nullptr;
+        BH_TRY(cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)));
+        const uint64_t l0 = c->launches;
+        enqueue_step();
+        c->graph_kernels[par] = c->launches - l0;  // counted when the graph runs, not when captured
+        c->launches = l0;
+        cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+        if (ce != cudaSuccess || !g) return cuda_status(ce == cudaSuccess ? cudaErrorUnknown : ce);
+        ce = cudaGraphInstantiate(&c->graph[par], g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+          c->graph[par] = nullptr;
+          return cuda_status(ce);
+        }
+        c->graph_keys0[par] = c->keys[0];
+      }
+      BH_TRY(cuda_status(cudaGraphLaunch(c->graph[par], c->stream)));
+      c->launches += c->graph_kernels[par];
       BH_TRY(last_launch());
       BH_TRY(sync_and_check(c, &e));
       if (e & bh::kErrNodes) {
@@ -858,9 +896,14 @@ bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* s
     uint32_t e = 0;
     for (;;) {
       const int par = c->cur;
+      if (c->graph[par] && c->graph_keys0[par]) {  // a plain step's graph: not this pipeline
+        cudaGraphExecDestroy(c->graph[par]);
+        c->graph[par] = nullptr;
+      }
       if (!c->graph[par]) {
         cudaGraph_t g = nullptr;
         BH_TRY(cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)));
+        c->graph_keys0[par] = nullptr;
         const uint64_t l0 = c->launches;
         enqueue_batch_step(c, *prm);
         c->graph_kernels[par] = c->launches - l0;  // counted when the graph runs, not when captured

@@ -168,6 +168,7 @@ struct bh_ctx {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // captured batched step, by state parity
   bh_params graph_params = {};
   uint64_t graph_kernels[2] = {0, 0};  // kernel launches inside each captured graph
+  uint64_t* graph_keys0[2] = {nullptr, nullptr};  // plain step graphs: the key buffer they were captured with
   uint64_t launches = 0;  // kernels launched on this context (every launcher adds its count)
 
   void* adj = nullptr;  // differentiable-path state (checkpoints, tape, adjoints): bh_adjoint.cu
