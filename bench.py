@@ -57,7 +57,10 @@ WORKLOADS = {
                                 "eps=0.001, leaf 8, dt=2e-4"),
 }
 METRIC = "body-steps/s @theta=0.5, acc err<=1e-3: plain vs batched/adjoint, 1 GB300 vs CPU"
-FLOPS_P2P, FLOPS_CELL_QUAD = 20, 57  # per interaction, see the design doc (FMA = 2 flops)
+# algorithmic flops per interaction (an FMA counts 2): point mass 20 (3 sub, r^2 + eps^2 6, rsqrt,
+# 2 mul, m d r^-3 6); quadrupole cell 57 (the point-mass terms plus Q.d 15, r^-5 2, update 6,
+# d.Q.d 5, scale 2, update 7)
+FLOPS_P2P, FLOPS_CELL_QUAD = 20, 57
 SORT_PASSES = 8
 
 
@@ -191,7 +194,7 @@ def ncu_traffic():
 
 def accuracy_vs_direct(w, pm, acc_by_theta, orc, nthreads, ntarget=1024, tree=None):
     """Median / p99 relative error of the step-0 accelerations against the FP64 direct sum on a
-    seeded subsample (the benchmark spec's <= 1e-3 gate), for the workload's theta and the others
+    seeded subsample (the <= 1e-3 accuracy gate at theta 0.5), for the workload's theta and the others
     of the at-scale sweep."""
     from oracle.oracle import relerr
 
