@@ -199,6 +199,9 @@ bh_status bh_batch_step(bh_ctx* ctx, const bh_params* params, int nsteps, bh_sta
 void bh_params_default(bh_params* p);
 
 bh_status bh_synchronize(bh_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t) and device, for callers that order their own
+ * work (or bh_sort_keys_static) with the library's: every call of the context runs on it. */
+bh_status bh_get_stream(bh_ctx* ctx, void** stream_out, int* device_out);
 
 /* CUDA events on the context's stream, for timing from the caller (slots 0..63). */
 bh_status bh_event_record(bh_ctx* ctx, int slot);

@@ -39,7 +39,7 @@ EXPORTS = [
     "bh_event_elapsed_ms", "bh_flush_l2", "bh_host_alloc", "bh_host_free", "bh_measure_fp32_peak",
     "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step", "bh_adjoint_forward",
     "bh_step_backward", "bh_energy_diag", "bh_autotune_walk", "bh_set_walk_variant", "bh_plummer_device",
-    "bh_batch_plummer_device", "bh_tree_boxes", "bh_save_snapshot", "bh_load_snapshot",
+    "bh_batch_plummer_device", "bh_tree_boxes", "bh_save_snapshot", "bh_load_snapshot", "bh_get_stream",
 ]
 
 
@@ -158,6 +158,7 @@ def load():
         "bh_tree_boxes": ([P, S, P, P, P], I),
         "bh_save_snapshot": ([P, ctypes.c_char_p], I),
         "bh_load_snapshot": ([P, ctypes.c_char_p], I),
+        "bh_get_stream": ([P, ctypes.POINTER(P), ctypes.POINTER(I)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -681,6 +681,13 @@ bh_status bh_synchronize(bh_ctx* c) {
   return cuda_status(cudaStreamSynchronize(c->stream));
 }
 
+bh_status bh_get_stream(bh_ctx* c, void** stream_out, int* device_out) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  if (stream_out) *stream_out = (void*)c->stream;
+  if (device_out) *device_out = c->device;
+  return BH_OK;
+}
+
 bh_status bh_event_record(bh_ctx* c, int slot) {
   if (!c || slot < 0 || slot >= bh::kNumEvents) return BH_ERR_INVALID_ARG;
   return cuda_status(cudaEventRecord(c->ev[slot], c->stream));
