@@ -505,6 +505,7 @@ using namespace bh;
 extern "C" {
 
 bh_status bh_adjoint_forward(bh_ctx* c, const bh_params* p, int nsteps, int checkpoint_every, bh_stats* st) {
+  bh::Range range_("bh_adjoint_forward");
   if (!c || !p || nsteps < 1 || checkpoint_every < 1 || c->batch || c->n == 0 ||
       p->multipole != BH_MULTIPOLE_QUADRUPOLE || !(p->eps > 0) || !(p->theta >= 0) || p->leaf_capacity < 1 ||
       !(p->edge_factor > 0))
@@ -580,6 +581,7 @@ bh_status bh_adjoint_forward(bh_ctx* c, const bh_params* p, int nsteps, int chec
 
 bh_status bh_step_backward(bh_ctx* c, const float* dl_dx4, const float* dl_dv4, float* grad_x4, float* grad_v4,
                            float* grad_m, bh_stats* st) {
+  bh::Range range_("bh_step_backward");
   if (!c || !c->adj) return BH_ERR_INVALID_ARG;
   AdjState* a = state(c);
   if (!a->valid || a->n != c->n) return BH_ERR_INVALID_ARG;

@@ -393,6 +393,7 @@ bh_status bh_sort_bodies(bh_ctx* c, uint32_t* perm_out) {
 }
 
 bh_status bh_build(bh_ctx* c, const double center[3], double edge, int leaf_capacity, int multipole) {
+  bh::Range range_("bh_build");
   if (!c || !center || !(edge > 0) || leaf_capacity < 1 ||
       (multipole != BH_MULTIPOLE_LITERAL && multipole != BH_MULTIPOLE_QUADRUPOLE))
     return BH_ERR_INVALID_ARG;
@@ -514,6 +515,7 @@ bh_status bh_node_lookup(bh_ctx* c, uint64_t key, bh_node* out) {
 }
 
 bh_status bh_force(bh_ctx* c, double theta, double eps, float* acc4_out, bh_stats* st) {
+  bh::Range range_("bh_force");
   if (!c || !(theta >= 0) || !(eps >= 0)) return BH_ERR_INVALID_ARG;
   if (!c->tree_valid) return BH_ERR_NO_TREE;
   cudaSetDevice(c->device);
@@ -560,6 +562,7 @@ bh_status bh_kick(bh_ctx* c, double dt) {
 }
 
 bh_status bh_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
+  bh::Range range_("bh_step");
   if (!c || !prm || nsteps < 0 || prm->leaf_capacity < 1 || !(prm->theta >= 0) || !(prm->eps >= 0) ||
       !(prm->edge_factor > 0) ||
       (prm->multipole != BH_MULTIPOLE_LITERAL && prm->multipole != BH_MULTIPOLE_QUADRUPOLE))
@@ -886,6 +889,7 @@ void reset_state(bh_ctx* c, size_t n) {
 extern "C" {
 
 bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
+  bh::Range range_("bh_batch_step");
   if (!c || !prm || nsteps < 0 || !c->batch || prm->leaf_capacity < 1 || !(prm->theta >= 0) || !(prm->eps >= 0) ||
       !(prm->edge_factor > 0) ||
       (prm->multipole != BH_MULTIPOLE_LITERAL && prm->multipole != BH_MULTIPOLE_QUADRUPOLE))
@@ -960,6 +964,7 @@ bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* s
 // Times every launch shape of the quadrupole walk on the tree in the arena (the last bh_step /
 // bh_build, or the last bh_batch_step) and keeps the fastest for this context.
 bh_status bh_autotune_walk(bh_ctx* c, double theta, double eps, int trials, bh_tune_result* out) {
+  bh::Range range_("bh_autotune_walk");
   if (!c || !out || !(theta >= 0) || !(eps > 0) || trials < 1) return BH_ERR_INVALID_ARG;
   const bool batch = c->batch;
   if (batch ? !c->batch_tree_ready : !c->tree_valid) return BH_ERR_NO_TREE;

@@ -136,6 +136,7 @@ using namespace bh;
 extern "C" {
 
 bh_status bh_energy_diag(bh_ctx* c, double theta, double eps, bh_energy* out, float* pot_out) {
+  bh::Range range_("bh_energy_diag");
   if (!c || !out || !(theta >= 0) || !(eps >= 0)) return BH_ERR_INVALID_ARG;
   if (!c->tree_valid) return BH_ERR_NO_TREE;
   cudaSetDevice(c->device);

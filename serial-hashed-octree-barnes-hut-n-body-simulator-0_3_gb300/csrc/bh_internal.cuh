@@ -1,11 +1,21 @@
 // Internal declarations shared by the libbhgpu translation units (not part of the ABI).
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include "bhgpu.h"
 
 namespace bh {
+
+// NVTX range over a host scope: names each library call in profiler timelines (header-only
+// NVTX 3; without an attached tool a push/pop is a no-op call).
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range&) = delete;
+  Range& operator=(const Range&) = delete;
+};
 
 constexpr int kMaxDepth = 21;             // 21 bits per axis, 63-bit keys (reference: MortonKeys.hpp:42)
 constexpr int kLevels = kMaxDepth + 1;    // depths 0..21
