@@ -311,6 +311,12 @@ bh_status bh_batch_plummer_device(bh_ctx* ctx, uint64_t seed, const uint32_t* sy
  * body count. Each output may be null; cap must be at least bh_tree_size. */
 bh_status bh_tree_boxes(bh_ctx* ctx, size_t cap, float* center_edge4, int32_t* depth, int64_t* count);
 
+/* Self-check of the bounded device wait (no counterpart in the reference): one thread polls a
+ * device flag (set to nonzero first when flag_set, else left zero so nothing ever sets it) at
+ * most `limit` times (<= 2^22, about a second) and gives up. Returns BH_OK when the flag was
+ * seen, BH_ERR_TIMEOUT when the wait ran out; the context stays usable either way. */
+bh_status bh_check_bounded_wait(bh_ctx* ctx, int flag_set, int limit);
+
 /* Snapshot files (no counterpart in the reference): the bodies (slot order), their
  * accelerations (so a run continues its leapfrog exactly) and, for an ensemble, the system
  * offsets. Loading replaces the context's state like bh_set_state / bh_batch_set. */

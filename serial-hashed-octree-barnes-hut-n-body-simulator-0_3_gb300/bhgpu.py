@@ -40,6 +40,7 @@ EXPORTS = [
     "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step", "bh_adjoint_forward",
     "bh_step_backward", "bh_energy_diag", "bh_autotune_walk", "bh_set_walk_variant", "bh_plummer_device",
     "bh_batch_plummer_device", "bh_tree_boxes", "bh_save_snapshot", "bh_load_snapshot", "bh_get_stream",
+    "bh_check_bounded_wait",
 ]
 
 
@@ -159,6 +160,7 @@ def load():
         "bh_save_snapshot": ([P, ctypes.c_char_p], I),
         "bh_load_snapshot": ([P, ctypes.c_char_p], I),
         "bh_get_stream": ([P, ctypes.POINTER(P), ctypes.POINTER(I)], I),
+        "bh_check_bounded_wait": ([P, I, I], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

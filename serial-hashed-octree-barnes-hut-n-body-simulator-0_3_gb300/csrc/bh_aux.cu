@@ -175,6 +175,18 @@ __global__ __launch_bounds__(kThreads) void k_node_boxes(const uint64_t* __restr
   if (count) count[i] = nrange[i].y;
 }
 
+// The bounded wait every device-side spin of the library uses (the sort's and the build's
+// look-backs): poll a word until it is nonzero, at most `limit` times with a short sleep, then
+// give up, set the timeout bit in the error word and return.
+__global__ void k_wait_flag(const uint32_t* __restrict__ flag, int limit, uint32_t* __restrict__ err) {
+  if (threadIdx.x != 0) return;
+  for (int i = 0; i < limit; ++i) {
+    if (*((volatile const uint32_t*)flag) != 0u) return;
+    __nanosleep(32);
+  }
+  atomicOr(err, kErrTimeout);
+}
+
 // Snapshot file: a 64-byte header, then pos_m (float4 x n), vel (float4 x n), acc (float4 x n)
 // and, for an ensemble, the system offsets (u32 x (nsys + 1)). Little-endian, as both host
 // architectures that run the library are.
@@ -248,6 +260,24 @@ bh_status bh_tree_boxes(bh_ctx* c, size_t cap, float* center_edge4, int32_t* dep
   dfree(dep);
   dfree(cnt);
   return s;
+}
+
+bh_status bh_check_bounded_wait(bh_ctx* c, int flag_set, int limit) {
+  if (!c || limit < 1 || limit > (1 << 22)) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  uint32_t* flag = nullptr;
+  BH_TRY(dalloc(&flag, 1));
+  clear_device_flags(c);
+  cudaMemsetAsync(flag, flag_set ? 0x01 : 0x00, sizeof(uint32_t), c->stream);
+  c->launches += 1;
+  k_wait_flag<<<1, 32, 0, c->stream>>>(flag, limit, c->err);
+  uint32_t e = 0;
+  bh_status s = last_launch();
+  if (s == BH_OK) s = sync_and_check(c, &e);
+  dfree(flag);
+  BH_TRY(s);
+  clear_device_flags(c);  // the context stays usable
+  return e ? err_to_status(e) : BH_OK;
 }
 
 bh_status bh_save_snapshot(bh_ctx* c, const char* path) {

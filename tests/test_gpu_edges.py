@@ -83,3 +83,18 @@ def test_adjoint_two_bodies_matches_direct_adjoint(bh, orc):
     assert np.allclose(gx[:, :3], rx, rtol=1e-4, atol=1e-6)
     assert np.allclose(gv[:, :3], rv, rtol=1e-4, atol=1e-6)
     assert np.allclose(gm, rm, rtol=1e-4, atol=1e-6)
+
+
+def test_bounded_wait_times_out_and_context_stays_usable(bh):
+    """A device wait on a flag that nothing sets gives up after its limit and reports
+    BH_ERR_TIMEOUT; the same context then waits successfully and still steps."""
+    lib = bh.load()
+    pm, vel = bh.plummer(2, 1000)
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1)
+    with bh.Simulation(1000) as sim:
+        assert lib.bh_check_bounded_wait(sim.h, 0, 20000) == 7  # BH_ERR_TIMEOUT
+        assert lib.bh_check_bounded_wait(sim.h, 1, 20000) == 0
+        assert lib.bh_check_bounded_wait(sim.h, 0, 0) == 1  # invalid limit
+        sim.set_bodies(pm, vel)
+        st = sim.step(prm, 2)
+        assert st.steps == 2 and st.error_flags == 0
