@@ -248,7 +248,8 @@ bh_status bh_create(bh_ctx** out, size_t capacity, int device) {
   if (s == BH_OK) s = dalloc(&c->sort.hist, 8 * 256);
   if (s == BH_OK) s = dalloc(&c->sort.lookback, (size_t)8 * c->sort.max_tiles * 256);
   if (s == BH_OK) s = dalloc(&c->sort.tile_ctr, 8);
-  c->lb_level_tiles = (int)((capacity + 255) / 256) + 1;
+  // tiles per level: 256 nodes each, or 8 each on the levels built one warp per node
+  c->lb_level_tiles = (int)std::max<size_t>((capacity + 255) / 256 + 1, kLevelWarpNodes / 8 + 1);
   if (s == BH_OK) s = dalloc(&c->lb_level, (size_t)kLevels * c->lb_level_tiles);
   if (s == BH_OK) s = dalloc(&c->level_bounds, kLevels + 2);
   if (s == BH_OK) s = dalloc(&c->level_tile_ctr, kLevels);

@@ -20,6 +20,9 @@ struct Range {
 constexpr int kMaxDepth = 21;             // 21 bits per axis, 63-bit keys (reference: MortonKeys.hpp:42)
 constexpr int kLevels = kMaxDepth + 1;    // depths 0..21
 constexpr int kNumEvents = 64;
+// Levels with at most this many nodes are built one warp per node (tiles of 8 nodes): one
+// resident wave of the build's 608 blocks x 8 warps.
+constexpr int kLevelWarpNodes = 4864;
 
 // Device error word bits. bit = (bh_status code - 3), so the host maps them back.
 enum : uint32_t {

@@ -441,6 +441,84 @@ __device__ __forceinline__ void split_search(const uint64_t* __restrict__ tkey, 
   for (int j = 0; j < K; ++j) bnd[2 * H * j + H] = a[j];
 }
 
+// Decoupled look-back over the tiles of one level (one thread): publishes the tile's child
+// count, sums the predecessors' counts back to the first inclusive prefix (eight predecessor
+// words per round trip, independent loads in flight together), publishes its own inclusive
+// prefix and returns the exclusive one. Waits are bounded; on expiry the timeout bit is set.
+__device__ uint32_t tile_lookback(uint32_t* __restrict__ lb, int tile, uint32_t btotal, uint32_t* __restrict__ err) {
+  uint32_t* mine = lb + tile;
+  st_relaxed(mine, (tile == 0 ? kLbPrefix : kLbAgg) | btotal);
+  uint32_t excl = 0;
+  if (tile == 0) return 0;
+  constexpr int kWin = 8;
+  int k = tile - 1, spins = 0;
+  while (k >= 0) {
+    uint32_t v[kWin];
+#pragma unroll
+    for (int q = 0; q < kWin; ++q)  // tile 0 always holds a prefix, so k - q < 0 is never consumed
+      v[q] = (k - q >= 0) ? ld_relaxed(lb + (k - q)) : kLbPrefix;
+    int used = 0;
+    bool done = false;
+#pragma unroll
+    for (int q = 0; q < kWin; ++q) {
+      if (done || used < q) continue;  // stop at a prefix or at the first unpublished tile
+      const uint32_t f = v[q] & ~kLbMask;
+      if (f == 0) continue;
+      excl += v[q] & kLbMask;
+      used = q + 1;
+      done = f == kLbPrefix;
+    }
+    if (done) break;
+    k -= used;
+    if (used == 0) {
+      if (++spins > kLbSpin) {
+        atomicOr(err, kErrTimeout);
+        break;
+      }
+      __nanosleep(32);
+    }
+  }
+  st_relaxed(mine, kLbPrefix | ((excl + btotal) & kLbMask));
+  return excl;
+}
+
+// The eight child ranges of one node by the whole warp: lanes 4(v-1) .. 4(v-1)+3 search for the
+// first index of [lo, hi) whose child digit is >= v (v = 1..7) with four probes per round, so
+// each round shrinks the interval about fivefold and the seven searches run together (about
+// log5 of the range in dependent loads instead of seven binary searches). Invariant per
+// search: every index below a has a smaller digit, and b is the answer or hi.
+__device__ __forceinline__ void warp_child_bounds(const uint64_t* __restrict__ tkey, int shift, int lo, int hi,
+                                                  int lane, int (&bnd)[9]) {
+  const int g = lane >> 2, k = lane & 3, v = g + 1;
+  const bool searcher = g < 7;
+  int a = lo, b = hi;
+  for (int it = 0; it < 40; ++it) {  // 40 rounds cover any 31-bit range
+    const bool big = searcher && (b - a > 4);
+    if (!__any_sync(0xffffffffu, big)) break;
+    const int step = (b - a) / 5;
+    bool ge = false;
+    if (big) ge = (int)((tkey[a + (k + 1) * step] >> shift) & 7ull) >= v;
+    const uint32_t grp = (__ballot_sync(0xffffffffu, ge) >> (4 * g)) & 0xFu;
+    if (big) {
+      if (grp) {
+        const int f = __ffs(grp) - 1;
+        b = a + (f + 1) * step;
+        if (f > 0) a = a + f * step + 1;
+      } else {
+        a = a + 4 * step + 1;
+      }
+    }
+  }
+  const bool probe = searcher && (a + k < b);
+  const bool ge = probe && (int)((tkey[a + k] >> shift) & 7ull) >= v;
+  const uint32_t grp = (__ballot_sync(0xffffffffu, ge) >> (4 * g)) & 0xFu;
+  const int ans = grp ? a + __ffs(grp) - 1 : b;
+  bnd[0] = lo;
+  bnd[8] = hi;
+#pragma unroll
+  for (int u = 1; u < 8; ++u) bnd[u] = __shfl_sync(0xffffffffu, ans, 4 * (u - 1));
+}
+
 __global__ __launch_bounds__(kThreads) void k_level(int d, const uint64_t* __restrict__ tkey, int leaf_cap,
                                                     uint64_t* __restrict__ nkey, int2* __restrict__ nrange,
                                                     WalkNode* __restrict__ wn, uint8_t* __restrict__ childbyte,
@@ -461,8 +539,70 @@ __global__ __launch_bounds__(kThreads) void k_level(int d, const uint64_t* __res
     if (blockIdx.x == 0 && t == 0) level_bounds[d + 2] = hi;
     return;
   }
-  const int ntiles = (count + kThreads - 1) / kThreads;
   const int shift = 3 * (kMaxDepth - 1 - d);
+  if (count <= kLevelWarpNodes) {
+    // few nodes with long body ranges (the top levels): one warp per node, tiles of one node
+    // per warp, the child ranges found by the warp-cooperative search
+    constexpr int kW = kThreads / 32;
+    const int ntiles_w = (count + kW - 1) / kW;
+    for (;;) {
+      if (t == 0) s_tile = atomicAdd(&tile_ctr[d], 1u);
+      __syncthreads();
+      const int tile = (int)s_tile;
+      __syncthreads();
+      if (tile >= ntiles_w) break;
+      const int node = lo + tile * kW + w;
+      const bool valid = node < hi;  // warp-uniform
+      int2 r = make_int2(0, 0);
+      bool internal = false;
+      int bnd[9];
+      int nc = 0;
+      uint32_t mask = 0;
+      if (valid) {
+        r = nrange[node];
+        internal = r.y > leaf_cap && d < kMaxDepth;
+        if (internal) {
+          warp_child_bounds(tkey, shift, r.x, r.x + r.y, lane, bnd);
+          for (int v = 0; v < 8; ++v)
+            if (bnd[v + 1] > bnd[v]) {
+              ++nc;
+              mask |= 1u << v;
+            }
+        }
+      }
+      if (lane == 0) s_warp[w] = (uint32_t)nc;
+      __syncthreads();
+      uint32_t wadd = 0, btotal = 0;
+      for (int i = 0; i < kW; ++i) {
+        if (i < w) wadd += s_warp[i];
+        btotal += s_warp[i];
+      }
+      if (t == 0) {
+        const uint32_t excl = tile_lookback(lb, tile, btotal, err);
+        s_excl = excl;
+        if (tile == ntiles_w - 1) level_bounds[d + 2] = hi + (int)(excl + btotal);
+      }
+      __syncthreads();
+      const long long child_base = (long long)hi + s_excl + wadd;
+      if (valid) {
+        const bool fits = child_base + nc <= node_cap;
+        if (!fits && lane == 0) atomicOr(err, kErrNodes);
+        const bool make = internal && fits;
+        if (make && lane < 8 && ((mask >> lane) & 1u)) {  // lane v writes child v
+          const int ci = (int)child_base + __popc(mask & ((1u << lane) - 1u));
+          nkey[ci] = (nkey[node] << 3) | (uint64_t)lane;
+          nrange[ci] = make_int2(bnd[lane], bnd[lane + 1] - bnd[lane]);
+        }
+        if (lane == 0) {
+          wn[node].link = make_int4(make ? (int)child_base : -1, make ? nc : 0, r.x, r.y);
+          childbyte[node] = (uint8_t)(make ? mask : 0u);
+        }
+      }
+      __syncthreads();
+    }
+    return;
+  }
+  const int ntiles = (count + kThreads - 1) / kThreads;
   for (;;) {
     if (t == 0) s_tile = atomicAdd(&tile_ctr[d], 1u);
     __syncthreads();
@@ -512,28 +652,7 @@ __global__ __launch_bounds__(kThreads) void k_level(int d, const uint64_t* __res
     const uint32_t my_excl = x - (uint32_t)nc + wadd;
     // tile look-back (thread 0)
     if (t == 0) {
-      uint32_t* mine = lb + tile;
-      st_relaxed(mine, (tile == 0 ? kLbPrefix : kLbAgg) | btotal);
-      uint32_t excl = 0;
-      if (tile > 0) {
-        int k = tile - 1, spins = 0;
-        while (k >= 0) {
-          uint32_t v = ld_relaxed(lb + k);
-          uint32_t f = v & ~kLbMask;
-          if (f == 0) {
-            if (++spins > kLbSpin) {
-              atomicOr(err, kErrTimeout);
-              break;
-            }
-            __nanosleep(32);
-            continue;
-          }
-          excl += v & kLbMask;
-          if (f == kLbPrefix) break;
-          --k;
-        }
-        st_relaxed(mine, kLbPrefix | ((excl + btotal) & kLbMask));
-      }
+      const uint32_t excl = tile_lookback(lb, tile, btotal, err);
       s_excl = excl;
       if (tile == ntiles - 1) level_bounds[d + 2] = hi + (int)(excl + btotal);
     }
