@@ -746,23 +746,41 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int
         min_rank = tslot[link.z];
         single = true;
       } else {
-        // unrolled so that several members' loads are in flight before the dependent sums
-#pragma unroll 4
-        for (int b = link.z; b < link.z + link.w; ++b) {
-          const float4 p = tpos[b];
-          mass = ff_add(mass, {p.w, 0.f});
-          com[0] = ff_add(com[0], ff_prod(p.x, p.w));
-          com[1] = ff_add(com[1], ff_prod(p.y, p.w));
-          com[2] = ff_add(com[2], ff_prod(p.z, p.w));
-          min_rank = min(min_rank, tslot[b]);
+        // members in batches of four: the batch's loads are issued together before the
+        // dependent float-float sums (same summation order as one member at a time)
+        const int end = link.z + link.w;
+        for (int b0 = link.z; b0 < end; b0 += 4) {
+          float4 pb[4];
+          uint32_t rb[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            pb[j] = b0 + j < end ? tpos[b0 + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            rb[j] = b0 + j < end ? tslot[b0 + j] : 0xffffffffu;
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (b0 + j >= end) break;
+            const float4 p = pb[j];
+            mass = ff_add(mass, {p.w, 0.f});
+            com[0] = ff_add(com[0], ff_prod(p.x, p.w));
+            com[1] = ff_add(com[1], ff_prod(p.y, p.w));
+            com[2] = ff_add(com[2], ff_prod(p.z, p.w));
+            min_rank = min(min_rank, rb[j]);
+          }
         }
         if (mass.hi != 0.f)
           for (int a = 0; a < 3; ++a) com[a] = ff_div(com[a], mass);
-#pragma unroll 4
-        for (int b = link.z; b < link.z + link.w; ++b) {
-          const float4 p = tpos[b];
-          quad_add(q, p.w, (p.x - com[0].hi) - com[0].lo, (p.y - com[1].hi) - com[1].lo,
-                   (p.z - com[2].hi) - com[2].lo);
+        for (int b0 = link.z; b0 < end; b0 += 4) {
+          float4 pb[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) pb[j] = b0 + j < end ? tpos[b0 + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (b0 + j >= end) break;
+            const float4 p = pb[j];
+            quad_add(q, p.w, (p.x - com[0].hi) - com[0].lo, (p.y - com[1].hi) - com[1].lo,
+                     (p.z - com[2].hi) - com[2].lo);
+          }
         }
       }
     } else {
@@ -776,6 +794,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int
           }
         }
       } else {
+        // (batching the children's loads like the leaf members' measured slower here)
         for (int c = link.x; c < link.x + link.y; ++c) {
           const NodeUp& ch = nf[c];
           const FF m = {ch.mass_hi, ch.mass_lo};
