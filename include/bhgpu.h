@@ -305,6 +305,38 @@ bh_status bh_plummer_device(bh_ctx* ctx, uint64_t seed, size_t n, double a, doub
 bh_status bh_batch_plummer_device(bh_ctx* ctx, uint64_t seed, const uint32_t* sys_offsets, size_t nsys,
                                   double a, double mtot);
 
+/* The reference app's own scene on the device (SetupSolarSystem, src/PhysicsHelpers.hpp:268-683;
+ * computeCartesianFromOrbital, src/SolarSystem.h:33-108): body 0 the Sun at rest at the origin,
+ * 1..8 Mercury..Neptune from the scene's orbital-element table (mean anomaly and gravitational
+ * parameter used as the reference uses them), 9 the Moon, then asteroids (a in 2.2-3.2 AU)
+ * while the index is below n / 2 and Oort-cloud comets (a in 1e3-1e5 AU) after. The random
+ * elements are the reference's ofRandom ranges, drawn from a counter-based generator per body
+ * (seed, body, draw) and rounded to float like ofRandom. units = BH_UNITS_SI keeps the
+ * reference's metres, kilograms and m/s; BH_UNITS_GRAVITATIONAL divides by AU, the solar mass
+ * and sqrt(G M_sun / AU), so the library's G = 1 force gives the scene's real dynamics (the SI
+ * quadrupoles of the Oort cloud, ~m r^2 ~ 1e49, exceed the FP32 range; SI scenes need the
+ * monopole-only literal mode). The state becomes these n bodies (like bh_set_bodies). */
+#define BH_UNITS_SI 0
+#define BH_UNITS_GRAVITATIONAL 1
+bh_status bh_solar_system_device(bh_ctx* ctx, uint64_t seed, size_t n, int units);
+
+/* Ephemeris ingest (host only): the records of a NASA JPL Horizons vector table, as
+ * parseHorizonsFilez (src/SolarSystem.c:411-700; EphemerisRecord, src/SolarSystem.h) finds them
+ * between the "$$SOE" and "$$EOE" lines: Julian date (TDB), X, Y, Z (km) and VX, VY, VZ (km/s).
+ * Record boundaries are the reference's. By default each value is the number after its label's
+ * '='; with BH_HORIZONS_LITERAL a value is read only from a token that starts with the label and
+ * holds the '=' (the reference's rule, under which Horizons' "X =-1.8E+08" layout reads as 0).
+ * *count receives the number of records; the first min(count, cap) go to out (which may be null
+ * to count only). Returns BH_ERR_INVALID_ARG for an unreadable file and BH_ERR_NOT_FOUND when
+ * the file has no $$SOE ... $$EOE region (the reference returns NULL with count 0). */
+typedef struct bh_ephemeris {
+  double jd_tdb;
+  double pos[3];
+  double vel[3];
+} bh_ephemeris;
+#define BH_HORIZONS_LITERAL 1
+bh_status bh_parse_horizons(const char* path, int flags, bh_ephemeris* out, size_t cap, size_t* count);
+
 /* Headless stand-in for the reference's node-box drawing (visualizeTree,
  * src/HashedOctree.cpp:939-974): for every node of the current tree (bh_build or the last
  * bh_step; node order of bh_tree_nodes) its cube as (centre x, y, z, edge), its depth and its

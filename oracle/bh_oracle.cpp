@@ -919,3 +919,146 @@ void orc_direct_adjoint(const double* pos3, const double* vel3, const double* ma
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// The reference app's solar-system scene (SetupSolarSystem, src/PhysicsHelpers.hpp:268-683),
+// restated in FP64 with the same random draws as the library's device generator.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+// The library's counter-based uniform in (0, 1): splitmix64's output mix of (seed, body, draw).
+uint64_t scene_mix(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+double scene_uniform(uint64_t seed, uint64_t body, uint32_t draw) {
+  const uint64_t z = scene_mix(scene_mix(seed + 0x9e3779b97f4a7c15ull * (body + 1)) ^ (0x632be59bd9b4e019ull * (draw + 1)));
+  return ((double)(z >> 11) + 0.5) * 0x1p-53;
+}
+// ofRandom(lo, hi) as a float: lo + (hi - lo) u, u the uniform rounded to float.
+float scene_draw(uint64_t seed, uint64_t body, uint32_t k, float lo, float hi) {
+  const float u = (float)scene_uniform(seed, body, k);
+  return lo + (hi - lo) * u;
+}
+
+const double kSceneG = 6.67430e-11, kSceneSun = 1.989e30, kSceneAU = 149597870700.0;
+const double kSceneDeg = 0.01745329252;  // toRadians, src/PhysicsHelpers.hpp:701-708
+
+// Newton from E = M until |step| <= 1e-10 (at most 100 steps), then the true anomaly and
+// calculatePositionAndVelocity (src/PhysicsHelpers.hpp:729-790).
+void scene_true_anomaly(double e, double a, double i, double node, double w, double M, double mu, double x[3],
+                        double v[3]) {
+  double E = M, delta;
+  int iter = 0;
+  do {
+    double f = E - e * std::sin(E) - M;
+    double fp = 1 - e * std::cos(E);
+    delta = -f / fp;
+    E += delta;
+    iter++;
+  } while (std::fabs(delta) > 1e-10 && iter < 100);
+  double nu = 2 * std::atan2(std::sqrt(1 + e) * std::sin(E / 2), std::sqrt(1 - e) * std::cos(E / 2));
+  double r = a * (1 - e * std::cos(E));
+  double xo = r * std::cos(nu), yo = r * std::sin(nu);
+  double cn = std::cos(node), sn = std::sin(node), cw = std::cos(w), sw = std::sin(w), ci = std::cos(i),
+         si = std::sin(i);
+  x[0] = xo * (cn * cw - sn * sw * ci) - yo * (cn * sw + sn * cw * ci);
+  x[1] = xo * (sn * cw + cn * sw * ci) + yo * (cn * cw * ci - sn * sw);
+  x[2] = xo * (sw * si) + yo * (cw * si);
+  double h = std::sqrt(mu * a * (1 - e * e));
+  double vxo = -mu / h * std::sin(nu), vyo = mu / h * (e + std::cos(nu));
+  v[0] = vxo * (cn * cw - sn * sw * ci) - vyo * (cn * sw + sn * cw * ci);
+  v[1] = vxo * (sn * cw + cn * sw * ci) + vyo * (cn * cw * ci - sn * sw);
+  v[2] = vxo * (sw * si) + vyo * (cw * si);
+}
+
+// computeCartesianFromOrbital (src/SolarSystem.h:33-108): 100 Newton steps, perifocal state,
+// rotation.
+void scene_eccentric(double a, double e, double i, double node, double w, double M, double mu, double x[3],
+                     double v[3]) {
+  double E = M;
+  for (int it = 0; it < 100; it++) {
+    double f = E - e * std::sin(E) - M;
+    double fp = 1.0 - e * std::cos(E);
+    E = E - f / fp;
+  }
+  double cE = std::cos(E), sE = std::sin(E), s1 = std::sqrt(1.0 - e * e);
+  double xp = a * (cE - e), yp = a * s1 * sE;
+  double n = std::sqrt(mu / (a * a * a));
+  double edot = n / (1.0 - e * cE);
+  double vxp = -a * edot * sE, vyp = a * edot * s1 * cE;
+  double cn = std::cos(node), sn = std::sin(node), ci = std::cos(i), si = std::sin(i), cw = std::cos(w),
+         sw = std::sin(w);
+  x[0] = (cn * cw - sn * sw * ci) * xp + (-cn * sw - sn * cw * ci) * yp;
+  x[1] = (sn * cw + cn * sw * ci) * xp + (-sn * sw + cn * cw * ci) * yp;
+  x[2] = (sw * si) * xp + (cw * si) * yp;
+  v[0] = (cn * cw - sn * sw * ci) * vxp + (-cn * sw - sn * cw * ci) * vyp;
+  v[1] = (sn * cw + cn * sw * ci) * vxp + (-sn * sw + cn * cw * ci) * vyp;
+  v[2] = (sw * si) * vxp + (cw * si) * vyp;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Scene of n bodies: out7[7 i ..] = x, y, z, vx, vy, vz, m in SI units (FP64, before any
+// rounding to the library's FP32 state).
+void orc_solar_system(uint64_t seed, size_t n, double* out7) {
+  // planet table of the scene (src/PhysicsHelpers.hpp:298-397): e, a (AU), i, node, periapsis
+  // (degrees), mean anomaly (used as radians), mass (kg, also used as mu)
+  static const double planets[8][7] = {
+      {0.205630, 0.387098, 7.00487, 48.331, 29.124, 174.795, 3.3011e23},
+      {0.006772, 0.723332, 3.39471, 76.6807, 54.8523, 50.416, 4.8675e24},
+      {0.016711, 1.000000, 0.00005, 348.73936, 114.20783, 357.51716, 5.97237e24},
+      {0.093394, 1.523679, 1.85061, 49.57854, 286.502, 19.3564, 6.4171e23},
+      {0.0489, 5.2026, 1.304, 100.464, 273.867, 20.02, 1.8982e27},
+      {0.0565, 9.5549, 2.485, 113.665, 339.392, 317.02, 5.6834e26},
+      {0.046381, 19.2184, 0.773, 74.006, 96.998857, 142.2386, 8.6810e25},
+      {0.008678, 30.1104, 1.767, 131.784, 273.187, 48.12369, 1.02413e26},
+  };
+  auto planet = [&](int p, double x[3], double v[3]) {
+    const double* q = planets[p];
+    scene_true_anomaly(q[0], q[1] * kSceneAU, q[2] * kSceneDeg, q[3] * kSceneDeg, q[4] * kSceneDeg, q[5], q[6], x,
+                       v);
+  };
+  for (size_t i = 0; i < n; ++i) {
+    double x[3] = {0, 0, 0}, v[3] = {0, 0, 0}, m = 0;
+    if (i == 0) {
+      m = kSceneSun;
+    } else if (i <= 8) {
+      planet((int)i - 1, x, v);
+      m = planets[i - 1][6];
+    } else if (i == 9) {
+      double xe[3], ve[3];
+      planet(2, xe, ve);
+      scene_true_anomaly(0.0549, 3.844e8, 5.145 * kSceneDeg, 125.08 * kSceneDeg, 318.15 * kSceneDeg, 135.27,
+                         kSceneG * 5.97237e24, x, v);
+      for (int k = 0; k < 3; ++k) {
+        x[k] += xe[k] * 1.1;
+        v[k] += ve[k];
+      }
+      m = 7.34767309e22;
+    } else {
+      const bool belt = (double)i < (double)n * 0.5;
+      const float e = belt ? scene_draw(seed, i, 0, 0.0f, 0.2f) : scene_draw(seed, i, 0, 0.8f, 0.99f);
+      const float a = belt ? scene_draw(seed, i, 1, 2.2f, 3.2f) : scene_draw(seed, i, 1, 1000.0f, 100000.0f);
+      const float inc = belt ? scene_draw(seed, i, 2, 0.0f, 15.0f) : scene_draw(seed, i, 2, 0.0f, 180.0f);
+      const float node = scene_draw(seed, i, 3, 0.0f, 360.0f);
+      const float w = scene_draw(seed, i, 4, 0.0f, 360.0f);
+      const float M = scene_draw(seed, i, 5, 0.0f, 360.0f);
+      const float mm = belt ? scene_draw(seed, i, 6, 1e15f, 1e21f) : scene_draw(seed, i, 6, 1e12f, 1e17f);
+      scene_eccentric((double)a * kSceneAU, e, inc * kSceneDeg, node * kSceneDeg, w * kSceneDeg, M * kSceneDeg,
+                      kSceneG * kSceneSun, x, v);
+      m = mm;
+    }
+    double* o = out7 + 7 * i;
+    for (int k = 0; k < 3; ++k) {
+      o[k] = x[k];
+      o[3 + k] = v[k];
+    }
+    o[6] = m;
+  }
+}
+
+}  // extern "C"

@@ -43,8 +43,38 @@ def build_ref():
     return out
 
 
+SOLAR_CXX = ["MathUtils.cpp", "Body.cpp"]
+SOLAR_C = ["SolarSystem.c", "StringUtilities.c", "FileUtilities.c", "DataExtraction.c", "GeneralUtilities.c",
+           "CommonDefinitions.c"]
+
+
+def build_ref_solar():
+    """REF-LITERAL for the app's scene set-up and ephemeris ingest: the reference's
+    SetupSolarSystem (src/PhysicsHelpers.hpp) and parseHorizonsFilez (src/SolarSystem.c) with
+    their C utilities, compiled unmodified against the shim, plus oracle/ref_solar_harness.cpp.
+    Returns the library path, or None when the reference checkout is absent."""
+    if not all(os.path.exists(os.path.join(REF_SRC, f)) for f in SOLAR_CXX + SOLAR_C + ["PhysicsHelpers.hpp"]):
+        return None
+    out_dir = os.path.join(HERE, "_ref")
+    obj_dir = os.path.join(out_dir, "obj")
+    os.makedirs(obj_dir, exist_ok=True)
+    objs = []
+    for f in SOLAR_C:
+        obj = os.path.join(obj_dir, f[:-2] + ".o")
+        pre = ["-include", os.path.join(HERE, "ref_shim", "isnan_int.h")] if f == "GeneralUtilities.c" else []
+        subprocess.run(["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fPIC", "-w", *pre, "-I" + REF_SRC, "-c",
+                        os.path.join(REF_SRC, f), "-o", obj], check=True)
+        objs.append(obj)
+    out = os.path.join(out_dir, "libbhref_solar.so")
+    cmd = ["g++", *FLAGS, "-w", "-I" + os.path.join(HERE, "ref_shim"), "-I" + REF_SRC, "-o", out + ".tmp",
+           os.path.join(HERE, "ref_solar_harness.cpp")] + [os.path.join(REF_SRC, f) for f in SOLAR_CXX] + objs
+    subprocess.run(cmd, check=True)
+    os.replace(out + ".tmp", out)
+    return out
+
+
 def build_all():
-    return build_restatement(), build_ref()
+    return build_restatement(), build_ref(), build_ref_solar()
 
 
 if __name__ == "__main__":

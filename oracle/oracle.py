@@ -7,6 +7,8 @@ baseline, as the checker or the timed CPU baseline. Never part of the product pa
                   restated in C++, FP64, with literal and intended multipole semantics.
     RefLiteral    oracle/_ref/libbhref.so: the reference's own compiled code (only where the
                   reference checkout was available at build time).
+    RefScene      oracle/_ref/libbhref_solar.so: the reference's own scene set-up and ephemeris
+                  parser (same condition).
 All positions are (n, 3) float64; masses (n,) float64.
 """
 import ctypes
@@ -17,6 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 RESTATEMENT_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libbhref.so")
+REF_SCENE_LIB = os.path.join(HERE, "_ref", "libbhref_solar.so")
 
 P, S, D, I, L = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double, ctypes.c_int, ctypes.c_long
 
@@ -58,7 +61,15 @@ class Restatement:
         lib.orc_frozen_entries.restype = L
         lib.orc_frozen_free.argtypes = [P]
         lib.orc_direct_adjoint.argtypes = [P, P, P, S, D, D, I, P, P, I, P, P, P, P, P]
+        lib.orc_solar_system.argtypes = [ctypes.c_uint64, S, P]
         self.lib = lib
+
+    def solar_system(self, seed, n):
+        """The reference app's scene (SetupSolarSystem) with the library's draws: (n, 7) float64
+        rows x, y, z, vx, vy, vz, m in SI units."""
+        out = np.zeros((n, 7))
+        self.lib.orc_solar_system(seed, n, _p(out))
+        return out
 
     def bounds(self, pos):
         pos = _f64(pos, 3)
@@ -287,6 +298,31 @@ class RefLiteral:
         rc = self.lib.ref_app_steps(_p(pos), _p(vel), _p(mass), len(pos), dt, theta, edge_factor, nsteps, _p(acc),
                                     _p(stage), _p(perm))
         return dict(pos=pos, vel=vel, mass=mass, acc=acc, perm=perm, stage_s=stage, rc=rc)
+
+
+class RefScene:
+    """The reference's own SetupSolarSystem and parseHorizonsFilez (REF-LITERAL)."""
+
+    def __init__(self, path=REF_SCENE_LIB):
+        if not os.path.exists(path):
+            raise RuntimeError(f"REF-LITERAL scene library not built: {path}")
+        lib = ctypes.CDLL(path)
+        lib.ref_solar_system.argtypes = [ctypes.c_uint64, S, P]
+        lib.ref_parse_horizons.argtypes = [ctypes.c_char_p, P, I]
+        lib.ref_parse_horizons.restype = I
+        self.lib = lib
+
+    def solar_system(self, seed, n):
+        out = np.zeros((n, 7))
+        self.lib.ref_solar_system(seed, n, _p(out))
+        return out
+
+    def parse_horizons(self, path):
+        """(count, 7) rows julianDate, position, velocity as the reference parses them."""
+        cap = 1 << 16
+        out = np.zeros((cap, 7))
+        cnt = self.lib.ref_parse_horizons(os.fsencode(path), _p(out), cap)
+        return out[:min(cnt, cap)].copy()
 
 
 def relerr(a, b):

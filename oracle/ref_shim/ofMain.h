@@ -41,5 +41,15 @@ inline void ofNoFill() {}
 template <class... A> inline void ofSetColor(A...) {}
 template <class... A> inline void ofDrawIcoSphere(A...) {}
 template <class... A> inline void ofDrawBox(A...) {}
-inline float ofRandom(float hi) { return hi * (float)std::rand() / (float)RAND_MAX; }
-inline float ofRandom(float lo, float hi) { return lo + (hi - lo) * (float)std::rand() / (float)RAND_MAX; }
+// A harness may install the generator behind ofRandom (the scene harness installs a
+// counter-based one so that the reference's set-up draws known numbers); by default rand().
+inline float (*&of_random_unit_hook())() {
+  static float (*hook)() = nullptr;
+  return hook;
+}
+inline float of_random_unit() {
+  return of_random_unit_hook() ? of_random_unit_hook()() : (float)std::rand() / (float)RAND_MAX;
+}
+inline float ofRandom(float hi) { return hi * of_random_unit(); }
+inline float ofRandom(float lo, float hi) { return lo + (hi - lo) * of_random_unit(); }
+inline float ofDegToRad(float deg) { return deg * (float)(PI / 180.0); }

@@ -40,7 +40,7 @@ EXPORTS = [
     "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step", "bh_adjoint_forward",
     "bh_step_backward", "bh_energy_diag", "bh_autotune_walk", "bh_set_walk_variant", "bh_plummer_device",
     "bh_batch_plummer_device", "bh_tree_boxes", "bh_save_snapshot", "bh_load_snapshot", "bh_get_stream",
-    "bh_check_bounded_wait",
+    "bh_check_bounded_wait", "bh_solar_system_device", "bh_parse_horizons",
 ]
 
 
@@ -161,6 +161,8 @@ def load():
         "bh_load_snapshot": ([P, ctypes.c_char_p], I),
         "bh_get_stream": ([P, ctypes.POINTER(P), ctypes.POINTER(I)], I),
         "bh_check_bounded_wait": ([P, I, I], I),
+        "bh_solar_system_device": ([P, ctypes.c_uint64, S, I], I),
+        "bh_parse_horizons": ([ctypes.c_char_p, I, P, S, ctypes.POINTER(S)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -188,6 +190,37 @@ def plummer(seed, n, a=1.0, mtot=1.0, pos_offset=None, vel_offset=None):
     vo = None if vel_offset is None else np.asarray(vel_offset, np.float64)
     check(lib.bh_plummer(seed, n, a, mtot, _ptr(po), _ptr(vo), _ptr(pm), _ptr(v)), "bh_plummer")
     return pm, v
+
+
+EPHEMERIS_DTYPE = np.dtype([("jd_tdb", np.float64), ("pos", np.float64, (3,)), ("vel", np.float64, (3,))])
+UNITS_SI, UNITS_GRAVITATIONAL = 0, 1
+HORIZONS_LITERAL = 1
+
+
+def parse_horizons(path, literal=False):
+    """Records of a NASA JPL Horizons vector table (bh_parse_horizons): a structured array with
+    fields jd_tdb, pos (km) and vel (km/s). literal=True applies the reference's token rule."""
+    lib = load()
+    cnt = ctypes.c_size_t(0)
+    flags = HORIZONS_LITERAL if literal else 0
+    check(lib.bh_parse_horizons(os.fsencode(path), flags, None, 0, ctypes.byref(cnt)), "bh_parse_horizons")
+    out = np.zeros(cnt.value, EPHEMERIS_DTYPE)
+    if cnt.value:
+        check(lib.bh_parse_horizons(os.fsencode(path), flags, _ptr(out), cnt.value, ctypes.byref(cnt)),
+              "bh_parse_horizons")
+    return out
+
+
+def bodies_from_ephemerides(tables, masses, record=0):
+    """Initial bodies from Horizons tables (one table per body, record `record` of each): SI
+    units (m, m/s, kg) as float32 (pos_m (k,4), vel (k,4))."""
+    pm = np.zeros((len(tables), 4), np.float32)
+    vel = np.zeros((len(tables), 4), np.float32)
+    for k, (t, m) in enumerate(zip(tables, masses)):
+        pm[k, :3] = t["pos"][record] * 1e3
+        pm[k, 3] = m
+        vel[k, :3] = t["vel"][record] * 1e3
+    return pm, vel
 
 
 def two_spheres(seed, n):
@@ -342,6 +375,10 @@ class Simulation:
         po = None if pos_offset is None else np.ascontiguousarray(pos_offset, np.float64)
         vo = None if vel_offset is None else np.ascontiguousarray(vel_offset, np.float64)
         check(self.lib.bh_plummer_device(self.h, seed, n, a, mtot, _ptr(po), _ptr(vo)), "bh_plummer_device")
+
+    def solar_system_device(self, seed, n, units=UNITS_SI):
+        """Generates the reference app's solar-system scene on the device (bh_solar_system_device)."""
+        check(self.lib.bh_solar_system_device(self.h, seed, n, units), "bh_solar_system_device")
 
     def batch_plummer_device(self, seed, offsets, a=1.0, mtot=1.0):
         """Generates an ensemble of Plummer spheres on the device (bh_batch_plummer_device)."""

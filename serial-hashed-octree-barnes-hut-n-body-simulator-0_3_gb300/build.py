@@ -14,7 +14,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libbhgpu.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["bh_api.cu", "bh_sort.cu", "bh_tree.cu", "bh_walk.cu", "bh_adjoint.cu", "bh_diag.cu", "bh_aux.cu", "bh_ic.cpp"]
+SOURCES = ["bh_api.cu", "bh_sort.cu", "bh_tree.cu", "bh_walk.cu", "bh_adjoint.cu", "bh_diag.cu", "bh_aux.cu", "bh_ic.cpp",
+           "bh_io.cpp"]
 
 
 def _nvcc():
@@ -26,8 +27,10 @@ def _nvcc():
 
 # Per-file flags. The walk flushes FP32 denormals to zero: every quantity it handles (positions,
 # masses, softened distances, multipoles) is many orders of magnitude above the denormal range,
-# and without denormal support rsqrtf and the FP32 arithmetic need fewer instructions.
-FILE_FLAGS = {"bh_walk.cu": ["-ftz=true"]}
+# and without denormal support rsqrtf and the FP32 arithmetic need fewer instructions. The
+# initial-condition generators keep every FP64 product and sum separately rounded, as the host
+# code they restate does (no contraction into fused multiply-adds).
+FILE_FLAGS = {"bh_walk.cu": ["-ftz=true"], "bh_aux.cu": ["-fmad=false"]}
 
 
 def _compile(src, extra):

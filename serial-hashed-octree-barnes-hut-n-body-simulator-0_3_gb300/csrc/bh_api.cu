@@ -630,6 +630,7 @@ bh_status bh_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
           return cuda_status(ce);
         }
         c->graph_keys0[par] = c->keys[0];
+        c->graph_n = c->n;
       }
       BH_TRY(cuda_status(cudaGraphLaunch(c->graph[par], c->stream)));
       c->launches += c->graph_kernels[par];
@@ -869,8 +870,11 @@ bh_status batch_layout(bh_ctx* c, const uint32_t* sys_offsets, size_t nsys) {
 }
 
 // A new state of n bodies in slot order 0..n-1: every derived structure (tree, ensemble layout,
-// captured graphs, recorded trajectory) is dropped; accelerations and Morton keys are zeroed. The
-// caller fills pos[0] / vel[0].
+// recorded trajectory) is dropped; accelerations and Morton keys are zeroed. The caller fills
+// pos[0] / vel[0]. Captured plain-step graphs stay valid for the same body count (they hold
+// only buffer pointers); as the two Morton key buffers are interchangeable while the keys are
+// zeroed, they are paired the way the state-0 graph was captured, so a reset followed by a
+// step replays that graph instead of capturing a new one.
 void reset_state(bh_ctx* c, size_t n) {
   c->n = n;
   c->cur = 0;
@@ -878,7 +882,10 @@ void reset_state(bh_ctx* c, size_t n) {
   c->batch = false;
   c->batch_tree_ready = false;
   adj_invalidate(c);
-  destroy_graphs(c);
+  if (n != c->graph_n)
+    destroy_graphs(c);
+  else if (c->graph[0] && c->graph_keys0[0] == c->body_key)
+    std::swap(c->body_key, c->keys[0]);
   if (n > 0) {
     cudaMemsetAsync(c->acc, 0, sizeof(float4) * n, c->stream);
     cudaMemsetAsync(c->body_key, 0, sizeof(uint64_t) * n, c->stream);

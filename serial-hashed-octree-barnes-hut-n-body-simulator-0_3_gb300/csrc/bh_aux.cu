@@ -146,6 +146,166 @@ bh_status generate(bh_ctx* c, uint64_t seed, int n, const uint32_t* off_dev, int
 }
 
 // ---------------------------------------------------------------------------------------
+// The reference's solar-system scene on the device (SetupSolarSystem,
+// src/PhysicsHelpers.hpp:268-683): slot 0 the Sun, 1..8 the planets, 9 the Moon, then an
+// asteroid belt up to n / 2 and an Oort cloud for the rest. One thread per body, FP64.
+// ---------------------------------------------------------------------------------------
+
+// Physical constants and the planet table of the scene (src/PhysicsHelpers.hpp:30-33,
+// 298-397): the orbital elements have to be the scene's own values. The mean anomaly is given
+// in degrees there but used as radians, and each planet's own mass is passed as the
+// gravitational parameter; both are kept, since they decide where the planets start.
+constexpr double kGrav = 6.67430e-11;
+constexpr double kSunMass = 1.989e30;
+constexpr double kAU = 149597870700.0;
+constexpr double kDegToRad = 0.01745329252;  // the reference's toRadians factor (src/PhysicsHelpers.hpp:701-708)
+
+struct PlanetElements {
+  double e, a_au, inc_deg, node_deg, peri_deg, mean, mass;
+};
+__constant__ PlanetElements kPlanets[8] = {
+    {0.205630, 0.387098, 7.00487, 48.331, 29.124, 174.795, 3.3011e23},         // Mercury
+    {0.006772, 0.723332, 3.39471, 76.6807, 54.8523, 50.416, 4.8675e24},         // Venus
+    {0.016711, 1.000000, 0.00005, 348.73936, 114.20783, 357.51716, 5.97237e24},  // Earth
+    {0.093394, 1.523679, 1.85061, 49.57854, 286.502, 19.3564, 6.4171e23},       // Mars
+    {0.0489, 5.2026, 1.304, 100.464, 273.867, 20.02, 1.8982e27},                // Jupiter
+    {0.0565, 9.5549, 2.485, 113.665, 339.392, 317.02, 5.6834e26},               // Saturn
+    {0.046381, 19.2184, 0.773, 74.006, 96.998857, 142.2386, 8.6810e25},         // Uranus
+    {0.008678, 30.1104, 1.767, 131.784, 273.187, 48.12369, 1.02413e26},         // Neptune
+};
+
+// Planets and the Moon (GetCartesianFromOrbitalRadians + calculatePositionAndVelocity,
+// src/PhysicsHelpers.hpp:729-811): Newton on Kepler's equation from E = M until the step is
+// at most 1e-10 (100 steps at most), true anomaly, radius, then the perifocal position and the
+// velocity (mu / h)(-sin nu, e + cos nu) rotated by (node, inclination, periapsis).
+__device__ void kepler_true_anomaly(double e, double a, double inc, double node, double peri, double mean,
+                                    double mu, double x[3], double v[3]) {
+  double E = mean, step;
+  int iter = 0;
+  do {
+    const double f = (E - e * sin(E)) - mean;
+    const double fp = 1.0 - e * cos(E);
+    step = -f / fp;
+    E += step;
+    ++iter;
+  } while (fabs(step) > 1e-10 && iter < 100);
+  const double nu = 2.0 * atan2(sqrt(1.0 + e) * sin(E / 2.0), sqrt(1.0 - e) * cos(E / 2.0));
+  const double r = a * (1.0 - e * cos(E));
+  const double cn = cos(node), sn = sin(node), cw = cos(peri), sw = sin(peri), ci = cos(inc), si = sin(inc);
+  // rotation columns applied to the perifocal x and y components
+  const double px = cn * cw - sn * sw * ci, qx = cn * sw + sn * cw * ci;
+  const double py = sn * cw + cn * sw * ci, qy = cn * cw * ci - sn * sw;
+  const double pz = sw * si, qz = cw * si;
+  const double xo = r * cos(nu), yo = r * sin(nu);
+  x[0] = xo * px - yo * qx;
+  x[1] = xo * py + yo * qy;
+  x[2] = xo * pz + yo * qz;
+  const double h = sqrt(mu * a * (1.0 - e * e));
+  const double vxo = -mu / h * sin(nu), vyo = mu / h * (e + cos(nu));
+  v[0] = vxo * px - vyo * qx;
+  v[1] = vxo * py + vyo * qy;
+  v[2] = vxo * pz + vyo * qz;
+}
+
+// Asteroids and comets (computeCartesianFromOrbital, src/SolarSystem.h:33-108): 100 Newton
+// steps from E = M, the perifocal position a (cos E - e, sqrt(1 - e^2) sin E) and velocity
+// a Edot (-sin E, sqrt(1 - e^2) cos E) with Edot = sqrt(mu / a^3) / (1 - e cos E), rotated by
+// Rz(node) Rx(inc) Rz(peri).
+__device__ void kepler_eccentric(double a, double e, double inc, double node, double peri, double mean, double mu,
+                                 double x[3], double v[3]) {
+  double E = mean;
+  for (int it = 0; it < 100; ++it) {
+    const double f = (E - e * sin(E)) - mean;
+    const double fp = 1.0 - e * cos(E);
+    E = E - f / fp;
+  }
+  const double cE = cos(E), sE = sin(E), s1 = sqrt(1.0 - e * e);
+  const double xp = a * (cE - e), yp = a * s1 * sE;
+  const double edot = sqrt(mu / (a * a * a)) / (1.0 - e * cE);
+  const double vxp = -a * edot * sE, vyp = a * edot * s1 * cE;
+  const double cn = cos(node), sn = sin(node), ci = cos(inc), si = sin(inc), cw = cos(peri), sw = sin(peri);
+  const double m00 = cn * cw - sn * sw * ci, m01 = -cn * sw - sn * cw * ci;
+  const double m10 = sn * cw + cn * sw * ci, m11 = -sn * sw + cn * cw * ci;
+  const double m20 = sw * si, m21 = cw * si;
+  x[0] = m00 * xp + m01 * yp;
+  x[1] = m10 * xp + m11 * yp;
+  x[2] = m20 * xp + m21 * yp;
+  v[0] = m00 * vxp + m01 * vyp;
+  v[1] = m10 * vxp + m11 * vyp;
+  v[2] = m20 * vxp + m21 * vyp;
+}
+
+// One draw of the scene's ofRandom(lo, hi) (a float): lo + (hi - lo) u in float arithmetic,
+// u the body's counter-based uniform rounded to float. Rounded explicitly, so no contraction
+// changes it.
+__device__ __forceinline__ float scene_draw(uint64_t seed, uint64_t body, uint32_t k, float lo, float hi) {
+  const float u = (float)uniform(seed, body, k);
+  return __fadd_rn(lo, __fmul_rn(__fsub_rn(hi, lo), u));
+}
+
+// Body i of the scene in SI units (m, m/s, kg). Belt and cloud bodies draw, in this order,
+// e, a, inclination, node, periapsis, mean anomaly (degrees) and mass from ofRandom ranges
+// (src/PhysicsHelpers.hpp:492-546).
+__device__ void scene_body(uint64_t seed, int i, int n, double x[3], double v[3], double* mass) {
+  x[0] = x[1] = x[2] = v[0] = v[1] = v[2] = 0.0;
+  if (i == 0) {
+    *mass = kSunMass;
+    return;
+  }
+  if (i <= 9) {
+    const bool moon = i == 9;
+    const PlanetElements& p = kPlanets[moon ? 2 : i - 1];
+    kepler_true_anomaly(p.e, p.a_au * kAU, p.inc_deg * kDegToRad, p.node_deg * kDegToRad, p.peri_deg * kDegToRad,
+                        p.mean, p.mass, x, v);
+    *mass = p.mass;
+    if (moon) {
+      // Earth-centred orbit with mu = G M_earth, moved by 1.1 x Earth's position and Earth's
+      // velocity (src/PhysicsHelpers.hpp:410-435)
+      double xm[3], vm[3];
+      kepler_true_anomaly(0.0549, 3.844e8, 5.145 * kDegToRad, 125.08 * kDegToRad, 318.15 * kDegToRad, 135.27,
+                          kGrav * 5.97237e24, xm, vm);
+      for (int k = 0; k < 3; ++k) {
+        x[k] = xm[k] + x[k] * 1.1;
+        v[k] = vm[k] + v[k];
+      }
+      *mass = 7.34767309e22;
+    }
+    return;
+  }
+  const bool belt = (double)i < (double)n * 0.5;
+  const float e = belt ? scene_draw(seed, i, 0, 0.0f, 0.2f) : scene_draw(seed, i, 0, 0.8f, 0.99f);
+  const float a = belt ? scene_draw(seed, i, 1, 2.2f, 3.2f) : scene_draw(seed, i, 1, 1000.0f, 100000.0f);
+  const float inc = belt ? scene_draw(seed, i, 2, 0.0f, 15.0f) : scene_draw(seed, i, 2, 0.0f, 180.0f);
+  const float node = scene_draw(seed, i, 3, 0.0f, 360.0f);
+  const float peri = scene_draw(seed, i, 4, 0.0f, 360.0f);
+  const float mean = scene_draw(seed, i, 5, 0.0f, 360.0f);
+  const float m = belt ? scene_draw(seed, i, 6, 1e15f, 1e21f) : scene_draw(seed, i, 6, 1e12f, 1e17f);
+  kepler_eccentric((double)a * kAU, (double)e, (double)inc * kDegToRad, (double)node * kDegToRad,
+                   (double)peri * kDegToRad, (double)mean * kDegToRad, kGrav * kSunMass, x, v);
+  *mass = (double)m;
+}
+
+// units: 0 = SI as the reference sets it up; 1 = AU, solar masses and the velocity unit of
+// G = 1 (sqrt(G M_sun / AU)), where the library's G = 1 force gives the real dynamics.
+__global__ __launch_bounds__(kThreads) void k_solar_system(int n, uint64_t seed, int units,
+                                                           float4* __restrict__ pos, float4* __restrict__ vel) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= n) return;
+  double x[3], v[3], m;
+  scene_body(seed, i, n, x, v, &m);
+  if (units == 1) {
+    const double vu = sqrt(kGrav * kSunMass / kAU);
+    for (int k = 0; k < 3; ++k) {
+      x[k] /= kAU;
+      v[k] /= vu;
+    }
+    m /= kSunMass;
+  }
+  pos[i] = make_float4((float)x[0], (float)x[1], (float)x[2], (float)m);
+  vel[i] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
+}
+
+// ---------------------------------------------------------------------------------------
 // node boxes
 // ---------------------------------------------------------------------------------------
 
@@ -229,6 +389,18 @@ bh_status bh_batch_plummer_device(bh_ctx* c, uint64_t seed, const uint32_t* sys_
   reset_state(c, n);
   BH_TRY(batch_layout(c, sys_offsets, nsys));
   return generate(c, seed, (int)n, c->sys_off, (int)nsys, a, mtot, nullptr);
+}
+
+bh_status bh_solar_system_device(bh_ctx* c, uint64_t seed, size_t n, int units) {
+  if (!c || n == 0 || n > c->cap || (units != BH_UNITS_SI && units != BH_UNITS_GRAVITATIONAL))
+    return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  reset_state(c, n);
+  c->launches += 1;
+  k_solar_system<<<(int)((n + kThreads - 1) / kThreads), kThreads, 0, c->stream>>>((int)n, seed, units, c->pos[0],
+                                                                                  c->vel[0]);
+  BH_TRY(last_launch());
+  return cuda_status(cudaStreamSynchronize(c->stream));
 }
 
 bh_status bh_tree_boxes(bh_ctx* c, size_t cap, float* center_edge4, int32_t* depth, int64_t* count) {

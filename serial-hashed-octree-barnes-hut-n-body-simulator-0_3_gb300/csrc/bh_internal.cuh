@@ -182,6 +182,7 @@ struct bh_ctx {
   bh_params graph_params = {};
   uint64_t graph_kernels[2] = {0, 0};  // kernel launches inside each captured graph
   uint64_t* graph_keys0[2] = {nullptr, nullptr};  // plain step graphs: the key buffer they were captured with
+  size_t graph_n = 0;                              // plain step graphs: the body count they were captured for
   uint64_t launches = 0;  // kernels launched on this context (every launcher adds its count)
 
   void* adj = nullptr;  // differentiable-path state (checkpoints, tape, adjoints): bh_adjoint.cu

@@ -98,3 +98,39 @@ def test_bounded_wait_times_out_and_context_stays_usable(bh):
         sim.set_bodies(pm, vel)
         st = sim.step(prm, 2)
         assert st.steps == 2 and st.error_flags == 0
+
+
+def test_reset_same_count_replays_identically(bh):
+    """A new state with the same body count keeps the captured step graphs (re-pairing the
+    Morton key buffers); the trajectory must be bit-identical to a fresh context's, also after
+    an odd number of steps, a different body count in between, and an ensemble in between."""
+    n = 3000
+    pm, vel = bh.plummer(5, n)
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1, edge_factor=2.0)
+
+    def run(sim, steps):
+        sim.set_bodies(pm, vel)
+        sim.step(prm, steps)
+        return sim.get_bodies()
+
+    with bh.Simulation(n) as fresh:
+        ref3 = run(fresh, 3)
+    with bh.Simulation(n) as fresh:
+        ref2 = run(fresh, 2)
+    with bh.Simulation(n) as sim:
+        for steps, ref in [(3, ref3), (3, ref3), (2, ref2), (3, ref3)]:
+            got = run(sim, steps)
+            for g, r in zip(got, ref):
+                assert np.array_equal(g, r)
+        pm2, vel2 = bh.plummer(6, n // 2)
+        sim.set_bodies(pm2, vel2)
+        sim.step(prm, 1)
+        got = run(sim, 3)
+        for g, r in zip(got, ref3):
+            assert np.array_equal(g, r)
+        sim.batch_set(np.concatenate([pm[: n // 2], pm2]), np.concatenate([vel[: n // 2], vel2]),
+                      [0, n // 2, n])
+        sim.batch_step(prm, 2)
+        got = run(sim, 3)
+        for g, r in zip(got, ref3):
+            assert np.array_equal(g, r)
