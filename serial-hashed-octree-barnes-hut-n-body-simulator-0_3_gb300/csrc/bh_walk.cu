@@ -373,23 +373,26 @@ __global__ __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) void k_walk(const W
           mixed = true;
         }
       }
-      // per-lane MAC for the mixed children, one ballot each
+      // per-lane MAC for the mixed children, one ballot each: the mixed children's barycentres
+      // and sizes are staged in shared memory (one broadcast load per child), and the child's
+      // own lane applies its open mask to the ballot
       uint32_t mixed_bits = __ballot_sync(0xffffffffu, mixed);
-      while (mixed_bits) {
-        const int j = __ffs(mixed_bits) - 1;
-        mixed_bits &= mixed_bits - 1;
-        const float cx = __shfl_sync(0xffffffffu, mac.x, j);
-        const float cy = __shfl_sync(0xffffffffu, mac.y, j);
-        const float cz = __shfl_sync(0xffffffffu, mac.z, j);
-        const float s2 = fabsf(__shfl_sync(0xffffffffu, mac.w, j));
-        const uint32_t m = __shfl_sync(0xffffffffu, pmask, j);
-        const float dx = cx - p.x, dy = cy - p.y, dz = cz - p.z;
-        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const uint32_t a = __ballot_sync(0xffffffffu, s2 < theta2 * d2) & m;
-        if (lane == j) {
-          am = a;
-          om = m & ~a;
-        }
+      if (mixed_bits) {
+        __syncwarp();
+        if (mixed) s.st0[lane] = make_float4(mac.x, mac.y, mac.z, fabsf(mac.w));
+        __syncwarp();
+        do {
+          const int j = __ffs(mixed_bits) - 1;
+          mixed_bits &= mixed_bits - 1;
+          const float4 cm = s.st0[j];
+          const float dx = cm.x - p.x, dy = cm.y - p.y, dz = cm.z - p.z;
+          const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          const uint32_t a = __ballot_sync(0xffffffffu, cm.w < theta2 * d2);
+          if (lane == j) {
+            am = a & pmask;
+            om = pmask & ~a;
+          }
+        } while (mixed_bits);
       }
 
       // ---- appends
