@@ -184,6 +184,19 @@ bh_status bh_kick(bh_ctx* ctx, double dt);
  * force -> kick. stats (optional) is filled for the call. */
 bh_status bh_step(bh_ctx* ctx, const bh_params* params, int nsteps, bh_stats* stats);
 
+/* One frame with the host arrays of a per-frame caller (the app's ofApp::update + draw over its
+ * Body array, src/ofApp.cpp:169-282): uploads positions+mass and velocities (n x 4 floats, the
+ * context's current slot order, i.e. as the previous download returned them) into the state,
+ * runs one bh_step, and downloads the new positions+mass and velocities (in the new slot order).
+ * The state keeps its accelerations, so a loop of calls is the same trajectory as bh_step.
+ * Any pointer may be null (no copy). With page-locked buffers (bh_host_alloc or registered
+ * memory) the copies overlap the step on a second stream: the velocity upload runs beside the
+ * bounds, keys and sort, the position download beside the tree build and walk; the step and its
+ * copies are one CUDA graph per state parity, re-captured when the buffers change. With pageable
+ * buffers the copies run before and after the step. */
+bh_status bh_step_host(bh_ctx* ctx, const bh_params* params, const float* pos_m4_in, const float* vel4_in,
+                       float* pos_m4_out, float* vel4_out, bh_stats* stats);
+
 /* Batched ensembles (no counterpart in the reference, which simulates one system): nsys
  * independent systems in one context, system s owning bodies [sys_offsets[s],
  * sys_offsets[s+1]) (host array of nsys + 1 entries, sys_offsets[0] = 0, every system non-empty,

@@ -40,7 +40,7 @@ EXPORTS = [
     "bh_plummer", "bh_sort_keys_static", "bh_batch_set", "bh_batch_step", "bh_adjoint_forward",
     "bh_step_backward", "bh_energy_diag", "bh_autotune_walk", "bh_set_walk_variant", "bh_plummer_device",
     "bh_batch_plummer_device", "bh_tree_boxes", "bh_save_snapshot", "bh_load_snapshot", "bh_get_stream",
-    "bh_check_bounded_wait", "bh_solar_system_device", "bh_parse_horizons",
+    "bh_check_bounded_wait", "bh_solar_system_device", "bh_parse_horizons", "bh_step_host",
 ]
 
 
@@ -163,6 +163,7 @@ def load():
         "bh_check_bounded_wait": ([P, I, I], I),
         "bh_solar_system_device": ([P, ctypes.c_uint64, S, I], I),
         "bh_parse_horizons": ([ctypes.c_char_p, I, P, S, ctypes.POINTER(S)], I),
+        "bh_step_host": ([P, ctypes.POINTER(Params), P, P, P, P, ctypes.POINTER(Stats)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -349,6 +350,19 @@ class Simulation:
         st = Stats()
         check(self.lib.bh_step(self.h, ctypes.byref(params), nsteps, ctypes.byref(st) if stats else None),
               "bh_step")
+        return st
+
+    def step_host(self, params, pos_in, vel_in, pos_out, vel_out, stats=True):
+        """One step with host copies (bh_step_host): numpy (n, 4) float32 arrays (or None);
+        page-locked arrays (PinnedArray.array) let the copies overlap the step."""
+        st = Stats()
+        args = []
+        for a in (pos_in, vel_in, pos_out, vel_out):
+            if a is not None:
+                assert a.dtype == np.float32 and a.flags.c_contiguous and a.shape == (self.n, 4)
+            args.append(_ptr(a))
+        check(self.lib.bh_step_host(self.h, ctypes.byref(params), *args, ctypes.byref(st) if stats else None),
+              "bh_step_host")
         return st
 
     def batch_set(self, pos_m, vel, offsets):

@@ -37,11 +37,12 @@ __global__ void k_iota(uint32_t* v, int n) {
 
 bh_status ensure_nodes(bh_ctx* c, size_t need) {
   if (c->node_cap >= need && c->nkey) return BH_OK;
-  for (auto& g : c->graph)  // captured graphs hold the old node pointers
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  for (int k = 0; k < 2; ++k)  // captured graphs hold the old node pointers
+    for (cudaGraphExec_t* g : {&c->graph[k], &c->host_graph[k]})
+      if (*g) {
+        cudaGraphExecDestroy(*g);
+        *g = nullptr;
+      }
   size_t cap = std::max<size_t>(need, 1024);
   dfree(c->nkey);
   dfree(c->nrange);
@@ -190,6 +191,11 @@ bh_status bh_destroy(bh_ctx* c) {
   dfree(c->hash_vals);
   for (auto& g : c->graph)
     if (g) cudaGraphExecDestroy(g);
+  for (auto& g : c->host_graph)
+    if (g) cudaGraphExecDestroy(g);
+  for (auto& e : c->io_ev)
+    if (e) cudaEventDestroy(e);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   bh::adj_release(c);
   dfree(c->sys_off);
   dfree(c->sys_geom);
@@ -562,81 +568,132 @@ bh_status bh_kick(bh_ctx* c, double dt) {
   return cuda_status(cudaStreamSynchronize(c->stream));
 }
 
-bh_status bh_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
-  bh::Range range_("bh_step");
-  if (!c || !prm || nsteps < 0 || prm->leaf_capacity < 1 || !(prm->theta >= 0) || !(prm->eps >= 0) ||
-      !(prm->edge_factor > 0) ||
-      (prm->multipole != BH_MULTIPOLE_LITERAL && prm->multipole != BH_MULTIPOLE_QUADRUPOLE))
-    return BH_ERR_INVALID_ARG;
-  cudaSetDevice(c->device);
-  if (st) std::memset(st, 0, sizeof(*st));
-  const int n = (int)c->n;
-  if (n == 0 || nsteps == 0) return BH_OK;
-  BH_TRY(ensure_nodes(c, initial_node_cap(c->n)));
+}  // extern "C"
+
+namespace {
+
+// Host buffers of bh_step_host (pinned; any may be null).
+struct HostIO {
+  const float* pos_in;
+  const float* vel_in;
+  float* pos_out;
+  float* vel_out;
+};
+
+bool pinned(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// One plain step enqueued on c->stream without host synchronisation (capturable). Stage events
+// are external event-record nodes when captured (a plain record during capture would only order
+// the capture, not record the event). With io, the copies run on c->copy_stream beside the step:
+// the velocities upload while bounds, keys and sort run; the positions, final after the drift,
+// download while the tree is built and walked; the velocities download after the walk's kick.
+void enqueue_plain_step(bh_ctx* c, const bh_params* prm, const HostIO* io) {
+  const int n = (int)c->n, cur = c->cur, nx = 1 - cur;
   const float dt = (float)prm->dt;
-  const uint64_t launches0 = c->launches;
-  // One step as a CUDA graph per state parity (the ping-pong buffers alternate), captured on
-  // first use and replayed: the step's ~70 launches cost one graph launch. Stage events are
-  // recorded inside the graph as external event-record nodes (a plain record during capture
-  // would only order the capture, not record the event).
+  const size_t bytes = sizeof(float4) * (size_t)n;
   auto mark = [&](int k) { cudaEventRecordWithFlags(c->stage_ev[k], c->stream, cudaEventRecordExternal); };
-  auto enqueue_step = [&]() {
-    const int nx = 1 - c->cur;
-    clear_device_flags(c);
-    mark(0);
-    bh::launch_bounds(c, c->pos[c->cur], n, prm->edge_factor);
-    mark(1);
-    bh::launch_morton(c, c->pos[c->cur], n, c->keys[0], c->vals[0]);
-    mark(2);
-    uint64_t* ko;
-    uint32_t* perm;
-    bh::radix_sort_pairs(c, c->keys[0], c->vals[0], c->keys[1], c->vals[1], n, c->stream, &ko, &perm);
-    mark(3);
-    bh::launch_gather_kd_treekey(c, perm, n, c->pos[c->cur], c->vel[c->cur], c->acc, prm->acc_follows_body, dt,
-                                 c->pos[nx], c->vel[nx], c->tkey, c->tslot);
-    mark(4);
-    enqueue_tree(c, c->pos[nx], n, prm->leaf_capacity, prm->multipole, true);
-    mark(5);
-    bh::launch_build(c, n, prm->leaf_capacity);
-    mark(6);
-    bh::launch_upsweep(c, n, prm->leaf_capacity, prm->multipole);
-    mark(7);
-    bh::launch_walk(c, n, (float)prm->theta, (float)prm->eps, prm->multipole, c->acc, c->vel[nx], 0.5f * dt);
-    mark(8);
-  };
+  if (io) {
+    cudaEventRecord(c->io_ev[0], c->stream);  // fork
+    cudaStreamWaitEvent(c->copy_stream, c->io_ev[0], 0);
+    if (io->vel_in) cudaMemcpyAsync(c->vel[cur], io->vel_in, bytes, cudaMemcpyHostToDevice, c->copy_stream);
+    cudaEventRecord(c->io_ev[1], c->copy_stream);
+    if (io->pos_in) cudaMemcpyAsync(c->pos[cur], io->pos_in, bytes, cudaMemcpyHostToDevice, c->stream);
+  }
+  clear_device_flags(c);
+  mark(0);
+  bh::launch_bounds(c, c->pos[cur], n, prm->edge_factor);
+  mark(1);
+  bh::launch_morton(c, c->pos[cur], n, c->keys[0], c->vals[0]);
+  mark(2);
+  uint64_t* ko;
+  uint32_t* perm;
+  bh::radix_sort_pairs(c, c->keys[0], c->vals[0], c->keys[1], c->vals[1], n, c->stream, &ko, &perm);
+  mark(3);
+  if (io) cudaStreamWaitEvent(c->stream, c->io_ev[1], 0);
+  bh::launch_gather_kd_treekey(c, perm, n, c->pos[cur], c->vel[cur], c->acc, prm->acc_follows_body, dt, c->pos[nx],
+                               c->vel[nx], c->tkey, c->tslot);
+  mark(4);
+  if (io) {
+    cudaEventRecord(c->io_ev[2], c->stream);
+    cudaStreamWaitEvent(c->copy_stream, c->io_ev[2], 0);
+    if (io->pos_out) cudaMemcpyAsync(io->pos_out, c->pos[nx], bytes, cudaMemcpyDeviceToHost, c->copy_stream);
+    cudaEventRecord(c->io_ev[3], c->copy_stream);
+  }
+  enqueue_tree(c, c->pos[nx], n, prm->leaf_capacity, prm->multipole, true);
+  mark(5);
+  bh::launch_build(c, n, prm->leaf_capacity);
+  mark(6);
+  bh::launch_upsweep(c, n, prm->leaf_capacity, prm->multipole);
+  mark(7);
+  bh::launch_walk(c, n, (float)prm->theta, (float)prm->eps, prm->multipole, c->acc, c->vel[nx], 0.5f * dt);
+  mark(8);
+  if (io) {
+    if (io->vel_out) cudaMemcpyAsync(io->vel_out, c->vel[nx], bytes, cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamWaitEvent(c->stream, c->io_ev[3], 0);  // join
+  }
+}
+
+bool same_io(const HostIO& a, const void* const b[4]) {
+  return a.pos_in == b[0] && a.vel_in == b[1] && a.pos_out == b[2] && a.vel_out == b[3];
+}
+
+// Runs nsteps plain steps, each one replay of a CUDA graph captured per state parity on first use
+// (the step's ~70 launches cost one graph launch). io (one step only) selects the graphs that
+// carry the host copies, captured per set of host buffers.
+bh_status run_plain_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st, const HostIO* io) {
+  BH_TRY(ensure_nodes(c, initial_node_cap(c->n)));
+  const uint64_t launches0 = c->launches;
   if (!same_params(c->graph_params, *prm)) destroy_graphs(c);
   c->graph_params = *prm;
   for (int s = 0; s < nsteps; ++s) {
     uint32_t e = 0;
     for (;;) {
       const int par = c->cur;
-      if (c->graph[par] && c->graph_keys0[par] != c->keys[0]) {  // the key buffers were swapped since
-        cudaGraphExecDestroy(c->graph[par]);
-        c->graph[par] = nullptr;
+      cudaGraphExec_t& graph = io ? c->host_graph[par] : c->graph[par];
+      uint64_t*& keys0 = io ? c->host_graph_keys0[par] : c->graph_keys0[par];
+      uint64_t& kernels = io ? c->host_graph_kernels[par] : c->graph_kernels[par];
+      // captured with other key buffers (they swap every step) or other host buffers
+      if (graph && (keys0 != c->keys[0] || (io && !same_io(*io, c->host_graph_ptrs[par])))) {
+        cudaGraphExecDestroy(graph);
+        graph = nullptr;
       }
-      if (!c->graph[par]) {
+      if (!graph) {
         cudaGraph_t g = nullptr;
         BH_TRY(cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)));
         const uint64_t l0 = c->launches;
-        enqueue_step();
-        c->graph_kernels[par] = c->launches - l0;  // counted when the graph runs, not when captured
+        enqueue_plain_step(c, prm, io);
+        kernels = c->launches - l0;  // counted when the graph runs, not when captured
         c->launches = l0;
         cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
         if (ce != cudaSuccess || !g) return cuda_status(ce == cudaSuccess ? cudaErrorUnknown : ce);
-        ce = cudaGraphInstantiate(&c->graph[par], g, 0);
+        ce = cudaGraphInstantiate(&graph, g, 0);
         cudaGraphDestroy(g);
         if (ce != cudaSuccess) {
-          c->graph[par] = nullptr;
+          graph = nullptr;
           return cuda_status(ce);
         }
-        c->graph_keys0[par] = c->keys[0];
+        keys0 = c->keys[0];
         c->graph_n = c->n;
+        if (io) {
+          c->host_graph_ptrs[par][0] = io->pos_in;
+          c->host_graph_ptrs[par][1] = io->vel_in;
+          c->host_graph_ptrs[par][2] = io->pos_out;
+          c->host_graph_ptrs[par][3] = io->vel_out;
+        }
       }
-      BH_TRY(cuda_status(cudaGraphLaunch(c->graph[par], c->stream)));
-      c->launches += c->graph_kernels[par];
+      BH_TRY(cuda_status(cudaGraphLaunch(graph, c->stream)));
+      c->launches += kernels;
       BH_TRY(last_launch());
       BH_TRY(sync_and_check(c, &e));
-      if (e & bh::kErrNodes) {
+      if (e & bh::kErrNodes) {  // arena too small: grow it (dropping the graphs) and redo the step
         BH_TRY(ensure_nodes(c, c->node_cap * 2));
         if (st) st->retries++;
         continue;
@@ -679,6 +736,48 @@ bh_status bh_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
   c->tree_edge = g.tedge;
   c->hash_valid = false;
   return last_launch();
+}
+
+bool valid_params(const bh_params* prm) {
+  return prm && prm->leaf_capacity >= 1 && prm->theta >= 0 && prm->eps >= 0 && prm->edge_factor > 0 &&
+         (prm->multipole == BH_MULTIPOLE_LITERAL || prm->multipole == BH_MULTIPOLE_QUADRUPOLE);
+}
+
+}  // namespace
+
+extern "C" {
+
+bh_status bh_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
+  bh::Range range_("bh_step");
+  if (!c || nsteps < 0 || !valid_params(prm)) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (c->n == 0 || nsteps == 0) return BH_OK;
+  return run_plain_steps(c, prm, nsteps, st, nullptr);
+}
+
+bh_status bh_step_host(bh_ctx* c, const bh_params* prm, const float* pos_m4_in, const float* vel4_in,
+                       float* pos_m4_out, float* vel4_out, bh_stats* st) {
+  bh::Range range_("bh_step_host");
+  if (!c || !valid_params(prm)) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (c->n == 0) return BH_OK;
+  const HostIO io{pos_m4_in, vel4_in, pos_m4_out, vel4_out};
+  if (!(pinned(pos_m4_in) && pinned(vel4_in) && pinned(pos_m4_out) && pinned(vel4_out))) {
+    // pageable buffers cannot be captured: copy, step, copy in order on the context's stream
+    const size_t bytes = sizeof(float4) * c->n;
+    if (pos_m4_in) cudaMemcpyAsync(c->pos[c->cur], pos_m4_in, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (vel4_in) cudaMemcpyAsync(c->vel[c->cur], vel4_in, bytes, cudaMemcpyHostToDevice, c->stream);
+    BH_TRY(run_plain_steps(c, prm, 1, st, nullptr));
+    return bh_get_bodies(c, pos_m4_out, vel4_out, nullptr);
+  }
+  if (!c->copy_stream) {
+    if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) return BH_ERR_DEVICE;
+    for (auto& e : c->io_ev)
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return BH_ERR_DEVICE;
+  }
+  return run_plain_steps(c, prm, 1, st, &io);
 }
 
 bh_status bh_synchronize(bh_ctx* c) {
@@ -772,11 +871,12 @@ namespace {
 constexpr size_t kMaxSystems = 65535;  // system ids are stored as u16
 
 void destroy_graphs(bh_ctx* c) {
-  for (auto& g : c->graph)
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  for (int k = 0; k < 2; ++k)
+    for (cudaGraphExec_t* g : {&c->graph[k], &c->host_graph[k]})
+      if (*g) {
+        cudaGraphExecDestroy(*g);
+        *g = nullptr;
+      }
 }
 
 bool same_params(const bh_params& a, const bh_params& b) {

@@ -183,6 +183,13 @@ struct bh_ctx {
   uint64_t graph_kernels[2] = {0, 0};  // kernel launches inside each captured graph
   uint64_t* graph_keys0[2] = {nullptr, nullptr};  // plain step graphs: the key buffer they were captured with
   size_t graph_n = 0;                              // plain step graphs: the body count they were captured for
+  // bh_step_host: the step with its host copies on a second stream, one graph per state parity
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t io_ev[4] = {};  // fork, velocities uploaded, positions final, positions downloaded
+  cudaGraphExec_t host_graph[2] = {nullptr, nullptr};
+  const void* host_graph_ptrs[2][4] = {};  // the host buffers each was captured with
+  uint64_t* host_graph_keys0[2] = {nullptr, nullptr};
+  uint64_t host_graph_kernels[2] = {0, 0};
   uint64_t launches = 0;  // kernels launched on this context (every launcher adds its count)
 
   void* adj = nullptr;  // differentiable-path state (checkpoints, tape, adjoints): bh_adjoint.cu

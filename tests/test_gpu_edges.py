@@ -134,3 +134,45 @@ def test_reset_same_count_replays_identically(bh):
         got = run(sim, 3)
         for g, r in zip(got, ref3):
             assert np.array_equal(g, r)
+
+
+def test_step_host_matches_step(bh):
+    """bh_step_host (upload, step, download; copies overlapped with page-locked buffers) follows
+    the same trajectory as bh_step, bit for bit: with page-locked buffers, with buffers that
+    change between calls (re-capture), with pageable numpy arrays, and with no copies at all."""
+    n = 5000
+    pm, vel = bh.plummer(8, n)
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1, edge_factor=2.0)
+    steps = 6
+    ref = []
+    with bh.Simulation(n) as a:
+        a.set_bodies(pm, vel)
+        for _ in range(steps):
+            a.step(prm, 1)
+            p, v, _ = a.get_bodies()
+            ref.append((p.copy(), v.copy()))
+    bufs = [[bh.PinnedArray((n, 4)) for _ in range(4)] for _ in range(2)]
+    try:
+        for mode in ("pinned", "alternating", "pageable", "none"):
+            with bh.Simulation(n) as b:
+                b.set_bodies(pm, vel)
+                p, v = pm.copy(), vel.copy()
+                for k in range(steps):
+                    if mode == "none":
+                        b.step_host(prm, None, None, None, None)
+                        p, v, _ = b.get_bodies()
+                    elif mode == "pageable":
+                        po, vo = np.zeros_like(p), np.zeros_like(v)
+                        b.step_host(prm, p, v, po, vo)
+                        p, v = po, vo
+                    else:
+                        pi, vi, po, vo = (x.array for x in bufs[k % 2 if mode == "alternating" else 0])
+                        pi[:] = p
+                        vi[:] = v
+                        b.step_host(prm, pi, vi, po, vo)
+                        p, v = po.copy(), vo.copy()
+                    assert np.array_equal(p, ref[k][0]) and np.array_equal(v, ref[k][1]), (mode, k)
+    finally:
+        for s in bufs:
+            for x in s:
+                x.free()
