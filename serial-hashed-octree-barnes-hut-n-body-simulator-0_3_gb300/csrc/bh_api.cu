@@ -49,6 +49,8 @@ bh_status ensure_nodes(bh_ctx* c, size_t need) {
   dfree(c->wnode);
   dfree(c->nup);
   dfree(c->nchildbyte);
+  dfree(c->nparent);
+  dfree(c->narrived);
   dfree(c->hash_keys);
   dfree(c->hash_vals);
   c->hash_cap = 0;
@@ -59,6 +61,8 @@ bh_status ensure_nodes(bh_ctx* c, size_t need) {
   BH_TRY(dalloc(&c->wnode, cap));
   BH_TRY(dalloc(&c->nup, cap));
   BH_TRY(dalloc(&c->nchildbyte, cap));
+  BH_TRY(dalloc(&c->nparent, cap));
+  BH_TRY(dalloc(&c->narrived, cap));
   c->node_cap = cap;
   c->tree_valid = false;
   return BH_OK;
@@ -184,6 +188,8 @@ bh_status bh_destroy(bh_ctx* c) {
   dfree(c->wnode);
   dfree(c->nup);
   dfree(c->nchildbyte);
+  dfree(c->nparent);
+  dfree(c->narrived);
   dfree(c->lb_level);
   dfree(c->level_bounds);
   dfree(c->level_tile_ctr);

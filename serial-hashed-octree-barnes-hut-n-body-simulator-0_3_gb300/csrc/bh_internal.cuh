@@ -141,6 +141,8 @@ struct bh_ctx {
   bh::WalkNode* wnode = nullptr;
   bh::NodeUp* nup = nullptr;
   uint8_t* nchildbyte = nullptr;
+  int* nparent = nullptr;      // parent node (-1 for roots), for the upsweep
+  uint32_t* narrived = nullptr;  // upsweep: children finished, per node
   uint32_t* lb_level = nullptr;  // look-back words of the level build
   int lb_level_tiles = 0;
   int* level_bounds = nullptr;  // [kLevels + 1] node index where each depth starts

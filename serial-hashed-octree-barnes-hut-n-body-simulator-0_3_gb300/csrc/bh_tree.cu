@@ -691,25 +691,41 @@ __device__ __forceinline__ void quad_add(float q[6], float m, float x, float y, 
   q[5] += fmaf(m3 * z, z, -r2m);
 }
 
-// One depth of the bottom-up multipole pass (computeTreeBaryCenters / computeNodeBaryCenters,
-// src/HashedOctree.cpp:721-855, as intended; or the literal pseudo-barycentres). Leaves
-// combine their member bodies, internal nodes their children (depth d + 1, done by the
-// previous launch).
-__global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int* __restrict__ level_bounds,
-                                                      const float4* __restrict__ tpos,
-                                                      const uint32_t* __restrict__ tslot,
-                                                      WalkNode* __restrict__ wn, NodeUp* __restrict__ nf,
-                                                      const Geom* __restrict__ g, const uint16_t* __restrict__ body_sys,
-                                                      const uint32_t* __restrict__ err, Counters* __restrict__ ctr) {
-  if (*err & kErrNodes) return;
-  const int lo = level_bounds[d], hi = level_bounds[d + 1];
-  if (hi <= lo) return;
-  const double edge0 = ldexp(g->tedge, -d);
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&ctr->max_depth, (unsigned)d);
-  for (int node = lo + blockIdx.x * kThreads + threadIdx.x; node < hi; node += gridDim.x * kThreads) {
+// A child's upsweep record as written by another thread of the same launch: read through L2
+// (an L1 line could hold a stale copy fetched for a neighbouring node).
+__device__ __forceinline__ NodeUp load_nodeup(const NodeUp* p) {
+  const float4* f = reinterpret_cast<const float4*>(p);
+  const float4 a = __ldcg(f), b = __ldcg(f + 1), c = __ldcg(f + 2), d = __ldcg(f + 3);
+  NodeUp u;
+  u.com_hi[0] = a.x;
+  u.com_hi[1] = a.y;
+  u.com_hi[2] = a.z;
+  u.mass_hi = a.w;
+  u.com_lo[0] = b.x;
+  u.com_lo[1] = b.y;
+  u.com_lo[2] = b.z;
+  u.mass_lo = b.w;
+  u.q[0] = c.x;
+  u.q[1] = c.y;
+  u.q[2] = c.z;
+  u.q[3] = c.w;
+  u.q[4] = d.x;
+  u.q[5] = d.y;
+  u.min_rank = __float_as_uint(d.z);
+  u.pad = __float_as_uint(d.w);
+  return u;
+}
+
+// The multipole of one node at depth d (computeTreeBaryCenters / computeNodeBaryCenters,
+// src/HashedOctree.cpp:721-855, as intended; or the literal pseudo-barycentres). A leaf
+// combines its member bodies, an internal node its children, whose records are complete.
+__device__ void upsweep_node(int node, int d, int mode, const float4* __restrict__ tpos,
+                             const uint32_t* __restrict__ tslot, WalkNode* __restrict__ wn, NodeUp* __restrict__ nf,
+                             const Geom* __restrict__ g, const uint16_t* __restrict__ body_sys) {
+  {
     const int4 link = wn[node].link;
     // batched ensembles: the node's system (that of its first body) sets the root edge
-    const double edge = body_sys ? ldexp(g[body_sys[link.z]].tedge, -d) : edge0;
+    const double edge = ldexp(body_sys ? g[body_sys[link.z]].tedge : g->tedge, -d);
     const float s2 = (float)(edge * edge);
     FF mass = {0.f, 0.f}, com[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     float q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -780,7 +796,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int
     } else {
       if (mode == BH_MULTIPOLE_LITERAL) {
         for (int c = link.x; c < link.x + link.y; ++c) {
-          const NodeUp& ch = nf[c];
+          const NodeUp ch = load_nodeup(nf + c);
           mass = ff_add(mass, {ch.mass_hi, ch.mass_lo});
           if (ch.min_rank < min_rank) {
             min_rank = ch.min_rank;
@@ -790,7 +806,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int
       } else {
         // (batching the children's loads like the leaf members' measured slower here)
         for (int c = link.x; c < link.x + link.y; ++c) {
-          const NodeUp& ch = nf[c];
+          const NodeUp ch = load_nodeup(nf + c);
           const FF m = {ch.mass_hi, ch.mass_lo};
           mass = ff_add(mass, m);
           for (int a = 0; a < 3; ++a) com[a] = ff_add(com[a], ff_mul({ch.com_hi[a], ch.com_lo[a]}, m));
@@ -799,7 +815,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int
         if (mass.hi != 0.f)
           for (int a = 0; a < 3; ++a) com[a] = ff_div(com[a], mass);
         for (int c = link.x; c < link.x + link.y; ++c) {
-          const NodeUp& ch = nf[c];
+          const NodeUp ch = load_nodeup(nf + c);
           quad_add(q, ch.mass_hi, (ch.com_hi[0] - com[0].hi) + (ch.com_lo[0] - com[0].lo),
                    (ch.com_hi[1] - com[1].hi) + (ch.com_lo[1] - com[1].lo),
                    (ch.com_hi[2] - com[2].hi) + (ch.com_lo[2] - com[2].lo));
@@ -823,6 +839,60 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int d, int mode, const int
     wn[node].mq = make_float4(mass.hi, q[0], q[1], q[2]);
     wn[node].q2 = make_float4(q[3], q[4], q[5], 0.f);
   }
+}
+
+// Parent links of the tree just built, and the arrival counters of the upsweep.
+__global__ __launch_bounds__(kThreads) void k_upsweep_links(const int* __restrict__ level_bounds,
+                                                            const WalkNode* __restrict__ wn, int* __restrict__ parent,
+                                                            uint32_t* __restrict__ arrived,
+                                                            const uint32_t* __restrict__ err) {
+  if (*err & kErrNodes) return;
+  const int m = level_bounds[kLevels], roots = level_bounds[1];
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < m; i += gridDim.x * kThreads) {
+    arrived[i] = 0u;
+    if (i < roots) parent[i] = -1;
+    const int4 link = wn[i].link;
+    for (int c = link.x; c < link.x + link.y; ++c) parent[c] = i;
+  }
+}
+
+// The bottom-up multipole pass in one launch. A thread per leaf computes the leaf, then climbs:
+// having published a node, it counts itself in at the parent; the thread
+// that completes the parent's count (the last of the children to finish) computes the parent
+// from all its children, in child order, and goes on up. Every node is computed once, from
+// complete children, with the arithmetic and order of a level-by-level pass, and no thread
+// ever waits for another.
+__global__ __launch_bounds__(kThreads) void k_upsweep(int mode, const int* __restrict__ level_bounds,
+                                                      const uint64_t* __restrict__ nkey,
+                                                      const int* __restrict__ parent, uint32_t* __restrict__ arrived,
+                                                      const float4* __restrict__ tpos,
+                                                      const uint32_t* __restrict__ tslot,
+                                                      WalkNode* __restrict__ wn, NodeUp* __restrict__ nf,
+                                                      const Geom* __restrict__ g, const uint16_t* __restrict__ body_sys,
+                                                      const uint32_t* __restrict__ err, Counters* __restrict__ ctr) {
+  if (*err & kErrNodes) return;
+  const int m = level_bounds[kLevels];
+  unsigned deepest = 0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < m; i += gridDim.x * kThreads) {
+    if (wn[i].link.y != 0) continue;  // internal: computed by its last child's thread
+    int node = i;
+    int d = (63 - __clzll((long long)nkey[i])) / 3;
+    deepest = max(deepest, (unsigned)d);
+    for (;;) {
+      upsweep_node(node, d, mode, tpos, tslot, wn, nf, g, body_sys);
+      const int p = parent[node];
+      if (p < 0) break;
+      // acquire-release: this node's stores are visible to the thread that completes the
+      // parent, and that thread sees every child's stores
+      unsigned prev;
+      asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(arrived + p) : "memory");
+      if (prev + 1u < (unsigned)wn[p].link.y) break;
+      node = p;
+      --d;
+    }
+  }
+  deepest = __reduce_max_sync(0xffffffffu, deepest);
+  if ((threadIdx.x & 31) == 0 && deepest > 0) atomicMax(&ctr->max_depth, deepest);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1085,12 +1155,14 @@ void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
 void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode, bool batch) {
   (void)leaf_cap;
   if (n <= 0) return;
-  const int grid = 152 * 8;
-  c->launches += kLevels;
-  for (int d = kMaxDepth; d >= 0; --d)
-    k_upsweep<<<grid, kThreads, 0, c->stream>>>(d, mode, c->level_bounds, c->tpos, c->tslot, c->wnode, c->nup,
-                                                batch ? c->sys_geom : c->geom, batch ? c->body_sys : nullptr,
-                                                c->err, c->counters);
+  // about a thread per node at N = 2^22 (grid 152 x 8 blocks, several leaves per thread: 0.39 ms;
+  // 152 x 32: 0.26 ms; the level-by-level pass it replaces: 0.29 ms)
+  const int grid = 152 * 32;
+  c->launches += 2;
+  k_upsweep_links<<<grid, kThreads, 0, c->stream>>>(c->level_bounds, c->wnode, c->nparent, c->narrived, c->err);
+  k_upsweep<<<grid, kThreads, 0, c->stream>>>(mode, c->level_bounds, c->nkey, c->nparent, c->narrived, c->tpos,
+                                              c->tslot, c->wnode, c->nup, batch ? c->sys_geom : c->geom,
+                                              batch ? c->body_sys : nullptr, c->err, c->counters);
 }
 
 void launch_batch_bounds(bh_ctx* c, const float4* pos, double edge_factor) {
