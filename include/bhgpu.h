@@ -207,6 +207,11 @@ bh_status bh_step_host(bh_ctx* ctx, const bh_params* params, const float* pos_m4
 bh_status bh_batch_set(bh_ctx* ctx, const float* pos_m4, const float* vel4, const uint32_t* sys_offsets,
                        size_t nsys);
 bh_status bh_batch_step(bh_ctx* ctx, const bh_params* params, int nsteps, bh_stats* stats);
+/* One batched step with host arrays, as bh_step_host does for one system: uploads positions+mass
+ * and velocities of all systems (n x 4 floats, the current slot order), steps, downloads them;
+ * with page-locked buffers the copies overlap the step. Requires bh_batch_set first. */
+bh_status bh_batch_step_host(bh_ctx* ctx, const bh_params* params, const float* pos_m4_in, const float* vel4_in,
+                             float* pos_m4_out, float* vel4_out, bh_stats* stats);
 
 /* Default parameters: theta 0.5, eps 0.025, dt 1e-3, leaf 1, quadrupole, edge 2, acc follows body. */
 void bh_params_default(bh_params* p);

@@ -41,6 +41,7 @@ EXPORTS = [
     "bh_step_backward", "bh_energy_diag", "bh_autotune_walk", "bh_set_walk_variant", "bh_plummer_device",
     "bh_batch_plummer_device", "bh_tree_boxes", "bh_save_snapshot", "bh_load_snapshot", "bh_get_stream",
     "bh_check_bounded_wait", "bh_solar_system_device", "bh_parse_horizons", "bh_step_host",
+    "bh_batch_step_host",
 ]
 
 
@@ -164,6 +165,7 @@ def load():
         "bh_solar_system_device": ([P, ctypes.c_uint64, S, I], I),
         "bh_parse_horizons": ([ctypes.c_char_p, I, P, S, ctypes.POINTER(S)], I),
         "bh_step_host": ([P, ctypes.POINTER(Params), P, P, P, P, ctypes.POINTER(Stats)], I),
+        "bh_batch_step_host": ([P, ctypes.POINTER(Params), P, P, P, P, ctypes.POINTER(Stats)], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -363,6 +365,18 @@ class Simulation:
             args.append(_ptr(a))
         check(self.lib.bh_step_host(self.h, ctypes.byref(params), *args, ctypes.byref(st) if stats else None),
               "bh_step_host")
+        return st
+
+    def batch_step_host(self, params, pos_in, vel_in, pos_out, vel_out, stats=True):
+        """One batched step with host copies (bh_batch_step_host); arrays as in step_host."""
+        st = Stats()
+        args = []
+        for a in (pos_in, vel_in, pos_out, vel_out):
+            if a is not None:
+                assert a.dtype == np.float32 and a.flags.c_contiguous and a.shape == (self.n, 4)
+            args.append(_ptr(a))
+        check(self.lib.bh_batch_step_host(self.h, ctypes.byref(params), *args, ctypes.byref(st) if stats else None),
+              "bh_batch_step_host")
         return st
 
     def batch_set(self, pos_m, vel, offsets):

@@ -586,6 +586,8 @@ struct HostIO {
   float* vel_out;
 };
 
+bh_status ensure_copy_stream(bh_ctx* c);  // the second stream of the *_step_host calls
+
 bool pinned(const void* p) {
   if (!p) return true;
   cudaPointerAttributes a{};
@@ -778,11 +780,7 @@ bh_status bh_step_host(bh_ctx* c, const bh_params* prm, const float* pos_m4_in, 
     BH_TRY(run_plain_steps(c, prm, 1, st, nullptr));
     return bh_get_bodies(c, pos_m4_out, vel4_out, nullptr);
   }
-  if (!c->copy_stream) {
-    if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) return BH_ERR_DEVICE;
-    for (auto& e : c->io_ev)
-      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return BH_ERR_DEVICE;
-  }
+  BH_TRY(ensure_copy_stream(c));
   return run_plain_steps(c, prm, 1, st, &io);
 }
 
@@ -891,9 +889,17 @@ bool same_params(const bh_params& a, const bh_params& b) {
 }
 
 // One batched step, enqueued on c->stream without host synchronisation (capturable).
-void enqueue_batch_step(bh_ctx* c, const bh_params& p) {
-  const int n = (int)c->n, nx = 1 - c->cur;
+void enqueue_batch_step(bh_ctx* c, const bh_params& p, const HostIO* io) {
+  const int n = (int)c->n, cur = c->cur, nx = 1 - cur;
   const float dt = (float)p.dt;
+  const size_t bytes = sizeof(float4) * (size_t)n;
+  if (io) {  // the copies of bh_batch_step_host, beside the step as in enqueue_plain_step
+    cudaEventRecord(c->io_ev[0], c->stream);
+    cudaStreamWaitEvent(c->copy_stream, c->io_ev[0], 0);
+    if (io->vel_in) cudaMemcpyAsync(c->vel[cur], io->vel_in, bytes, cudaMemcpyHostToDevice, c->copy_stream);
+    cudaEventRecord(c->io_ev[1], c->copy_stream);
+    if (io->pos_in) cudaMemcpyAsync(c->pos[cur], io->pos_in, bytes, cudaMemcpyHostToDevice, c->stream);
+  }
   clear_device_flags(c);
   bh::launch_batch_bounds(c, c->pos[c->cur], p.edge_factor);
   bh::launch_morton(c, c->pos[c->cur], n, c->keys[0], c->vals[0], true);
@@ -903,8 +909,15 @@ void enqueue_batch_step(bh_ctx* c, const bh_params& p) {
   bh::launch_sys_keys(c, c->vals[0], n, c->keys[1]);
   bh::radix_sort_pairs(c, c->keys[1], c->vals[0], c->keys[0], c->vals[1], n, c->stream, &ko, &vo, 0, 2);
   // vals[0]: (system, Morton key) order; keys[0] receives the per-slot tree keys
-  bh::launch_gather_kd_treekey(c, c->vals[0], n, c->pos[c->cur], c->vel[c->cur], c->acc, p.acc_follows_body, dt,
+  if (io) cudaStreamWaitEvent(c->stream, c->io_ev[1], 0);
+  bh::launch_gather_kd_treekey(c, c->vals[0], n, c->pos[cur], c->vel[cur], c->acc, p.acc_follows_body, dt,
                                c->pos[nx], c->vel[nx], c->keys[0], c->tslot, true);
+  if (io) {
+    cudaEventRecord(c->io_ev[2], c->stream);
+    cudaStreamWaitEvent(c->copy_stream, c->io_ev[2], 0);
+    if (io->pos_out) cudaMemcpyAsync(io->pos_out, c->pos[nx], bytes, cudaMemcpyDeviceToHost, c->copy_stream);
+    cudaEventRecord(c->io_ev[3], c->copy_stream);
+  }
   cudaMemcpyAsync(c->tkey, c->keys[0], sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, c->stream);
   bh::radix_sort_pairs(c, c->tkey, c->tslot, c->keys[1], c->vals[1], n, c->stream, &ko, &vo);
   bh::launch_sys_keys(c, c->tslot, n, c->keys[1]);
@@ -913,6 +926,10 @@ void enqueue_batch_step(bh_ctx* c, const bh_params& p) {
   bh::launch_build(c, n, p.leaf_capacity, true);
   bh::launch_upsweep(c, n, p.leaf_capacity, p.multipole, true);
   bh::launch_walk(c, n, (float)p.theta, (float)p.eps, p.multipole, c->acc, c->vel[nx], 0.5f * dt, true);
+  if (io) {
+    if (io->vel_out) cudaMemcpyAsync(io->vel_out, c->vel[nx], bytes, cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamWaitEvent(c->stream, c->io_ev[3], 0);  // join
+  }
 }
 
 }  // namespace
@@ -1002,15 +1019,13 @@ void reset_state(bh_ctx* c, size_t n) {
 
 extern "C" {
 
-bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
-  bh::Range range_("bh_batch_step");
-  if (!c || !prm || nsteps < 0 || !c->batch || prm->leaf_capacity < 1 || !(prm->theta >= 0) || !(prm->eps >= 0) ||
-      !(prm->edge_factor > 0) ||
-      (prm->multipole != BH_MULTIPOLE_LITERAL && prm->multipole != BH_MULTIPOLE_QUADRUPOLE))
-    return BH_ERR_INVALID_ARG;
-  cudaSetDevice(c->device);
-  if (st) std::memset(st, 0, sizeof(*st));
-  if (c->n == 0 || nsteps == 0) return BH_OK;
+}  // extern "C"
+
+namespace {
+
+// nsteps batched steps, each one replay of a graph captured per state parity; with io (one
+// step) the graphs that carry the host copies, captured per set of host buffers.
+bh_status run_batch_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st, const HostIO* io) {
   const size_t need = std::max<size_t>(2 * c->n + 64 * (size_t)c->nsys, 1024);
   if (c->node_cap < need) destroy_graphs(c);
   BH_TRY(ensure_nodes(c, need));
@@ -1021,30 +1036,40 @@ bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* s
     uint32_t e = 0;
     for (;;) {
       const int par = c->cur;
-      if (c->graph[par] && c->graph_keys0[par]) {  // a plain step's graph: not this pipeline
-        cudaGraphExecDestroy(c->graph[par]);
-        c->graph[par] = nullptr;
+      cudaGraphExec_t& graph = io ? c->host_graph[par] : c->graph[par];
+      uint64_t*& keys0 = io ? c->host_graph_keys0[par] : c->graph_keys0[par];
+      uint64_t& kernels = io ? c->host_graph_kernels[par] : c->graph_kernels[par];
+      // a plain step's graph (it records its key buffer), or other host buffers
+      if (graph && (keys0 || (io && !same_io(*io, c->host_graph_ptrs[par])))) {
+        cudaGraphExecDestroy(graph);
+        graph = nullptr;
       }
-      if (!c->graph[par]) {
+      if (!graph) {
         cudaGraph_t g = nullptr;
         BH_TRY(cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)));
-        c->graph_keys0[par] = nullptr;
+        keys0 = nullptr;
         const uint64_t l0 = c->launches;
-        enqueue_batch_step(c, *prm);
-        c->graph_kernels[par] = c->launches - l0;  // counted when the graph runs, not when captured
+        enqueue_batch_step(c, *prm, io);
+        kernels = c->launches - l0;  // counted when the graph runs, not when captured
         c->launches = l0;
         cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
         if (ce != cudaSuccess || !g) return cuda_status(ce == cudaSuccess ? cudaErrorUnknown : ce);
-        ce = cudaGraphInstantiate(&c->graph[par], g, 0);
+        ce = cudaGraphInstantiate(&graph, g, 0);
         cudaGraphDestroy(g);
         if (ce != cudaSuccess) {
-          c->graph[par] = nullptr;
+          graph = nullptr;
           return cuda_status(ce);
+        }
+        if (io) {
+          c->host_graph_ptrs[par][0] = io->pos_in;
+          c->host_graph_ptrs[par][1] = io->vel_in;
+          c->host_graph_ptrs[par][2] = io->pos_out;
+          c->host_graph_ptrs[par][3] = io->vel_out;
         }
       }
       if (st) cudaEventRecord(c->stage_ev[0], c->stream);
-      BH_TRY(cuda_status(cudaGraphLaunch(c->graph[par], c->stream)));
-      c->launches += c->graph_kernels[par];
+      BH_TRY(cuda_status(cudaGraphLaunch(graph, c->stream)));
+      c->launches += kernels;
       if (st) cudaEventRecord(c->stage_ev[1], c->stream);
       BH_TRY(sync_and_check(c, &e));
       if (e & bh::kErrNodes) {  // arena too small: grow it, re-capture, redo the step
@@ -1073,6 +1098,46 @@ bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* s
   c->hash_valid = false;
   c->batch_tree_ready = nsteps > 0;
   return last_launch();
+}
+
+bh_status ensure_copy_stream(bh_ctx* c) {
+  if (c->copy_stream) return BH_OK;
+  if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) return BH_ERR_DEVICE;
+  for (auto& e : c->io_ev)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return BH_ERR_DEVICE;
+  return BH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+bh_status bh_batch_step(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st) {
+  bh::Range range_("bh_batch_step");
+  if (!c || nsteps < 0 || !c->batch || !valid_params(prm)) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (c->n == 0 || nsteps == 0) return BH_OK;
+  return run_batch_steps(c, prm, nsteps, st, nullptr);
+}
+
+bh_status bh_batch_step_host(bh_ctx* c, const bh_params* prm, const float* pos_m4_in, const float* vel4_in,
+                             float* pos_m4_out, float* vel4_out, bh_stats* st) {
+  bh::Range range_("bh_batch_step_host");
+  if (!c || !c->batch || !valid_params(prm)) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  if (st) std::memset(st, 0, sizeof(*st));
+  if (c->n == 0) return BH_OK;
+  const HostIO io{pos_m4_in, vel4_in, pos_m4_out, vel4_out};
+  if (!(pinned(pos_m4_in) && pinned(vel4_in) && pinned(pos_m4_out) && pinned(vel4_out))) {
+    const size_t bytes = sizeof(float4) * c->n;
+    if (pos_m4_in) cudaMemcpyAsync(c->pos[c->cur], pos_m4_in, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (vel4_in) cudaMemcpyAsync(c->vel[c->cur], vel4_in, bytes, cudaMemcpyHostToDevice, c->stream);
+    BH_TRY(run_batch_steps(c, prm, 1, st, nullptr));
+    return bh_get_bodies(c, pos_m4_out, vel4_out, nullptr);
+  }
+  BH_TRY(ensure_copy_stream(c));
+  return run_batch_steps(c, prm, 1, st, &io);
 }
 
 // Times every launch shape of the quadrupole walk on the tree in the arena (the last bh_step /

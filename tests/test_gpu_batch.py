@@ -70,3 +70,44 @@ def test_batch_set_rejects_bad_offsets(bh):
         for off in ([0, 50, 50, 100], [1, 100], [0, 60, 40, 100]):
             with pytest.raises(bh.BHError):
                 sim.batch_set(pm, vel, np.array(off, np.uint32))
+
+
+def test_batch_step_host_matches_batch_step(bh):
+    """bh_batch_step_host (host copies beside the batched step) follows bh_batch_step's
+    trajectory bit for bit, with page-locked and with pageable buffers, also after a plain step
+    on the same context (its step graphs must not be reused for the ensemble)."""
+    pm, vel, off = ensemble(bh, 23, 3, 50, 2000)
+    n = len(pm)
+    prm = bh.default_params(theta=0.6, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1, edge_factor=2.0)
+    steps = 4
+    ref = []
+    with bh.Simulation(n) as a:
+        a.batch_set(pm, vel, off)
+        for _ in range(steps):
+            a.batch_step(prm, 1)
+            p, v, _ = a.get_bodies()
+            ref.append((p.copy(), v.copy()))
+    bufs = [bh.PinnedArray((n, 4)) for _ in range(4)]
+    try:
+        for mode in ("pinned", "pageable", "after_plain"):
+            with bh.Simulation(n) as b:
+                if mode == "after_plain":
+                    b.set_bodies(pm, vel)
+                    b.step_host(prm, bufs[0].array, bufs[1].array, bufs[2].array, bufs[3].array)
+                b.batch_set(pm, vel, off)
+                p, v = pm.copy(), vel.copy()
+                for k in range(steps):
+                    if mode == "pageable":
+                        po, vo = np.zeros_like(p), np.zeros_like(v)
+                        b.batch_step_host(prm, p, v, po, vo)
+                        p, v = po, vo
+                    else:
+                        pi, vi, po, vo = (x.array for x in bufs)
+                        pi[:] = p
+                        vi[:] = v
+                        b.batch_step_host(prm, pi, vi, po, vo)
+                        p, v = po.copy(), vo.copy()
+                    assert np.array_equal(p, ref[k][0]) and np.array_equal(v, ref[k][1]), (mode, k)
+    finally:
+        for x in bufs:
+            x.free()
