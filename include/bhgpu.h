@@ -32,8 +32,8 @@
  *     same FP32 positions.
  *   - The body order inside a context is the order of the last bh_sort_bodies / bh_step
  *     (Morton order), as in the reference after RadixSortBodies.
- *   - All work runs on one GPU, on the context's own CUDA stream. Calls that return data to
- *     the host synchronise that stream.
+ *   - All work runs on one GPU, on the context's CUDA stream (its own, or the caller's after
+ *     bh_set_stream). Calls that return data to the host synchronise that stream.
  */
 #ifndef BHGPU_H
 #define BHGPU_H
@@ -220,6 +220,11 @@ bh_status bh_synchronize(bh_ctx* ctx);
 /* The context's CUDA stream (a cudaStream_t) and device, for callers that order their own
  * work (or bh_sort_keys_static) with the library's: every call of the context runs on it. */
 bh_status bh_get_stream(bh_ctx* ctx, void** stream_out, int* device_out);
+/* Runs the context's work on the caller's stream (a cudaStream_t of the context's device) from
+ * now on, after finishing the work already queued; NULL returns to the context's own stream.
+ * The caller keeps ownership of its stream and must not destroy it while the context uses it.
+ * Step graphs are still captured on the context's own stream and launched on this one. */
+bh_status bh_set_stream(bh_ctx* ctx, void* stream);
 
 /* CUDA events on the context's stream, for timing from the caller (slots 0..63). */
 bh_status bh_event_record(bh_ctx* ctx, int slot);

@@ -41,7 +41,7 @@ EXPORTS = [
     "bh_step_backward", "bh_energy_diag", "bh_autotune_walk", "bh_set_walk_variant", "bh_plummer_device",
     "bh_batch_plummer_device", "bh_tree_boxes", "bh_save_snapshot", "bh_load_snapshot", "bh_get_stream",
     "bh_check_bounded_wait", "bh_solar_system_device", "bh_parse_horizons", "bh_step_host",
-    "bh_batch_step_host",
+    "bh_batch_step_host", "bh_set_stream",
 ]
 
 
@@ -161,6 +161,7 @@ def load():
         "bh_save_snapshot": ([P, ctypes.c_char_p], I),
         "bh_load_snapshot": ([P, ctypes.c_char_p], I),
         "bh_get_stream": ([P, ctypes.POINTER(P), ctypes.POINTER(I)], I),
+        "bh_set_stream": ([P, P], I),
         "bh_check_bounded_wait": ([P, I, I], I),
         "bh_solar_system_device": ([P, ctypes.c_uint64, S, I], I),
         "bh_parse_horizons": ([ctypes.c_char_p, I, P, S, ctypes.POINTER(S)], I),

@@ -215,7 +215,7 @@ bh_status bh_destroy(bh_ctx* c) {
   if (c->h_err) cudaFreeHost(c->h_err);
   if (c->h_counters) cudaFreeHost(c->h_counters);
   if (c->h_level_bounds) cudaFreeHost(c->h_level_bounds);
-  if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return BH_OK;
 }
@@ -239,7 +239,8 @@ bh_status bh_create(bh_ctx** out, size_t capacity, int device) {
     bh_destroy(c);
     return s;
   };
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(BH_ERR_DEVICE);
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return fail(BH_ERR_DEVICE);
+  c->stream = c->own_stream;
   for (auto& e : c->ev)
     if (cudaEventCreate(&e) != cudaSuccess) return fail(BH_ERR_DEVICE);
   for (auto& e : c->stage_ev)
@@ -588,6 +589,16 @@ struct HostIO {
 
 bh_status ensure_copy_stream(bh_ctx* c);  // the second stream of the *_step_host calls
 
+// Step graphs are captured on the context's own stream (a caller's stream may be one that
+// cannot be captured, such as the legacy default stream) and launched on c->stream; the guard
+// points c->stream at the own stream for the capture and restores it on every exit.
+struct CaptureOnOwnStream {
+  bh_ctx* c;
+  cudaStream_t saved;
+  explicit CaptureOnOwnStream(bh_ctx* ctx) : c(ctx), saved(ctx->stream) { c->stream = c->own_stream; }
+  ~CaptureOnOwnStream() { c->stream = saved; }
+};
+
 bool pinned(const void* p) {
   if (!p) return true;
   cudaPointerAttributes a{};
@@ -674,6 +685,7 @@ bh_status run_plain_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats*
         graph = nullptr;
       }
       if (!graph) {
+        CaptureOnOwnStream on_own(c);
         cudaGraph_t g = nullptr;
         BH_TRY(cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)));
         const uint64_t l0 = c->launches;
@@ -787,6 +799,14 @@ bh_status bh_step_host(bh_ctx* c, const bh_params* prm, const float* pos_m4_in, 
 bh_status bh_synchronize(bh_ctx* c) {
   if (!c) return BH_ERR_INVALID_ARG;
   return cuda_status(cudaStreamSynchronize(c->stream));
+}
+
+bh_status bh_set_stream(bh_ctx* c, void* stream) {
+  if (!c) return BH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  BH_TRY(cuda_status(cudaStreamSynchronize(c->stream)));
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return BH_OK;
 }
 
 bh_status bh_get_stream(bh_ctx* c, void** stream_out, int* device_out) {
@@ -1045,6 +1065,7 @@ bh_status run_batch_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats*
         graph = nullptr;
       }
       if (!graph) {
+        CaptureOnOwnStream on_own(c);
         cudaGraph_t g = nullptr;
         BH_TRY(cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)));
         keys0 = nullptr;

@@ -115,7 +115,8 @@ struct bh_ctx {
   int device = 0;
   size_t cap = 0;  // bodies
   size_t n = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // where the context's work runs (own_stream or the caller's)
+  cudaStream_t own_stream = nullptr;  // created with the context; every graph capture runs on it
   cudaEvent_t ev[bh::kNumEvents] = {};
   cudaEvent_t stage_ev[16] = {};
 

@@ -176,3 +176,35 @@ def test_step_host_matches_step(bh):
         for s in bufs:
             for x in s:
                 x.free()
+
+
+def test_caller_stream(bh):
+    """bh_set_stream: the context's work runs on a caller's stream (here one made by PyTorch,
+    used only as a stream factory) and the trajectory is the same as on the context's own
+    stream; NULL returns to the own stream. The stream handle round-trips through
+    bh_get_stream."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+
+    n = 4000
+    pm, vel = bh.plummer(11, n)
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1, edge_factor=2.0)
+    with bh.Simulation(n) as a:
+        a.set_bodies(pm, vel)
+        a.step(prm, 4)
+        ref = a.get_bodies()
+    lib = bh.load()
+    user = torch.cuda.Stream()
+    with bh.Simulation(n) as b:
+        b.set_bodies(pm, vel)
+        b.step(prm, 1)  # captures the state-0 graph on the own stream
+        assert lib.bh_set_stream(b.h, ctypes.c_void_p(user.cuda_stream)) == 0
+        got_stream = ctypes.c_void_p()
+        assert lib.bh_get_stream(b.h, ctypes.byref(got_stream), None) == 0
+        assert got_stream.value == user.cuda_stream
+        b.step(prm, 2)  # one new capture (state 1) while the caller's stream is set
+        assert lib.bh_set_stream(b.h, None) == 0
+        b.step(prm, 1)
+        got = b.get_bodies()
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
