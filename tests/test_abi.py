@@ -82,3 +82,28 @@ def test_two_spheres_layout(bh):
     assert np.allclose(b[:, :3].mean(0), (10, 0, 0), atol=1e-4)
     assert np.isclose(b[:, 3].sum(), 0.1, rtol=1e-5) and np.isclose(a[:, 3].sum(), 1.0, rtol=1e-5)
     assert np.allclose(v[2000:, :3].mean(0), (-0.3, 0.1, 0), atol=1e-5)
+
+
+def test_every_entry_point_rejects_null_arguments(bh):
+    """The reference throws std::invalid_argument on null pointers; every entry point of the C ABI
+    returns BH_ERR_INVALID_ARG for a null context or null required pointers instead, before
+    touching a device (so this runs without a GPU)."""
+    lib = bh.load()
+    exempt = {
+        "bh_status_string": None,       # returns a name
+        "bh_params_default": None,      # fills a struct, ignores null
+        "bh_host_free": 0,              # freeing null is a no-op, as free() does
+        "bh_sort_keys_static": None,    # n = 0 on the caller's stream: needs a device to decide
+    }
+    for name in bh.EXPORTS:
+        f = getattr(lib, name)
+        args = []
+        for t in f.argtypes:
+            pointer = t in (ctypes.c_void_p, ctypes.c_char_p) or t.__name__.startswith("LP_")
+            args.append(None if pointer else t(0))
+        rc = f(*args)
+        if name in exempt:
+            if exempt[name] is not None:
+                assert rc == exempt[name], name
+            continue
+        assert rc == 1, (name, rc)
