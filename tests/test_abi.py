@@ -50,6 +50,7 @@ def test_invalid_arguments(bh):
     lib = bh.load()
     h = ctypes.c_void_p()
     assert lib.bh_create(ctypes.byref(h), 0, 0) == 1
+    assert lib.bh_create(ctypes.byref(h), 1 << 30, 0) == 1  # above the 2^30 - 1 bodies the sort counts
     assert lib.bh_create(None, 10, 0) == 1
     assert lib.bh_destroy(None) == 1
     assert lib.bh_step(None, None, 1, None) == 1
