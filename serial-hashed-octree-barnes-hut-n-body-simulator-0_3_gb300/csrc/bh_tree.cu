@@ -5,6 +5,8 @@
 // intrinsics (__dadd_rn, __dmul_rn, ...), so the compiler cannot contract it into FMAs.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "bh_internal.cuh"
 
 namespace bh {
@@ -1155,9 +1157,11 @@ void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
 void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode, bool batch) {
   (void)leaf_cap;
   if (n <= 0) return;
-  // about a thread per node at N = 2^22 (grid 152 x 8 blocks, several leaves per thread: 0.39 ms;
-  // 152 x 32: 0.26 ms; the level-by-level pass it replaces: 0.29 ms)
-  const int grid = 152 * 32;
+  // a thread for every two bodies, about one per node or more at leaf capacity >= 2 (the climbs
+  // want a thread per leaf: at N = 2^22 a fixed 152 x 8 blocks took 0.39 ms, this 0.27 ms, the
+  // level-by-level pass it replaces 0.29 ms; at N = 2^25 a fixed 152 x 32 blocks took 2.65 ms,
+  // this 1.54 ms)
+  const int grid = std::max(152 * 8, (n / 2 + kThreads - 1) / kThreads);
   c->launches += 2;
   k_upsweep_links<<<grid, kThreads, 0, c->stream>>>(c->level_bounds, c->wnode, c->nparent, c->narrived, c->err);
   k_upsweep<<<grid, kThreads, 0, c->stream>>>(mode, c->level_bounds, c->nkey, c->nparent, c->narrived, c->tpos,
