@@ -155,6 +155,11 @@ bh_status bh_compute_bounds(bh_ctx* ctx, bh_bounds* out);
  * reference stores them in Body::bodyKey) and are copied to keys_out when it is not null. */
 bh_status bh_morton_keys(bh_ctx* ctx, double size, uint64_t* keys_out);
 
+/* decodeMortonKey (src/MortonKeys.hpp:204-228) for n caller keys (host arrays: n u64 in,
+ * 3n doubles out), on the context's device: each axis's 21 bits de-interleaved and mapped back
+ * to x_int / 2^21 * 2 * size - size, bit for bit the reference's FP64 result. */
+bh_status bh_decode_morton_keys(bh_ctx* ctx, const uint64_t* keys, size_t n, double size, double* pos3_out);
+
 /* RadixSortBodies: stable sort of the bodies by their current keys. perm_out (optional)
  * receives, per new slot, the previous slot of the body. Like the reference, the
  * acceleration array is not reordered. */

@@ -1062,3 +1062,18 @@ void orc_solar_system(uint64_t seed, size_t n, double* out7) {
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// decodeMortonKey (src/MortonKeys.hpp:204-228): the 21 bits of each axis de-interleaved from the
+// key (x from bits 3i + 2, y from 3i + 1, z from 3i), then x_int / 2^21 * 2 * size - size.
+void orc_decode_morton(const uint64_t* keys, size_t n, double size, double* pos3) {
+  for (size_t i = 0; i < n; ++i) {
+    uint64_t q[3] = {0, 0, 0};
+    for (int b = 0; b < 21; ++b)
+      for (int a = 0; a < 3; ++a) q[a] |= ((keys[i] >> (3 * b + 2 - a)) & 1ull) << b;
+    for (int a = 0; a < 3; ++a) pos3[3 * i + a] = (double)q[a] / 2097152.0 * 2.0 * size - size;
+  }
+}
+
+}  // extern "C"

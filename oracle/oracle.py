@@ -62,7 +62,14 @@ class Restatement:
         lib.orc_frozen_free.argtypes = [P]
         lib.orc_direct_adjoint.argtypes = [P, P, P, S, D, D, I, P, P, I, P, P, P, P, P]
         lib.orc_solar_system.argtypes = [ctypes.c_uint64, S, P]
+        lib.orc_decode_morton.argtypes = [P, S, D, P]
         self.lib = lib
+
+    def decode_morton(self, keys, size):
+        keys = np.ascontiguousarray(keys, np.uint64)
+        out = np.zeros((len(keys), 3))
+        self.lib.orc_decode_morton(_p(keys), len(keys), size, _p(out))
+        return out
 
     def solar_system(self, seed, n):
         """The reference app's scene (SetupSolarSystem) with the library's draws: (n, 7) float64
@@ -231,7 +238,14 @@ class RefLiteral:
         lib.ref_build_nodes.restype = L
         lib.ref_force.argtypes = [P, P, S, P, D, D, P, P]
         lib.ref_app_steps.argtypes = [P, P, P, S, D, D, D, I, P, P, P]
+        lib.ref_decode_morton.argtypes = [P, S, D, P]
         self.lib = lib
+
+    def decode_morton(self, keys, size):
+        keys = np.ascontiguousarray(keys, np.uint64)
+        out = np.zeros((len(keys), 3))
+        self.lib.ref_decode_morton(_p(keys), len(keys), size, _p(out))
+        return out
 
     def bounds(self, pos):
         pos = _f64(pos, 3)

@@ -11,6 +11,7 @@
 // Entry points and the reference code each one drives:
 //   ref_bounds        OctantBounds::OctantBounds(Body*, size_t)        src/OctantUtils.cpp:27-59
 //   ref_morton_keys   computeMortonKey                                 src/MortonKeys.hpp:137-181
+//   ref_decode_morton decodeMortonKey                                  src/MortonKeys.hpp:204-228
 //   ref_sort_bodies   RadixSortBodies                                  src/Body.hpp:275-302
 //   ref_guard         DetermineOctant / GetChildKey / HOTNode child ctor src/OctantUtils.hpp:64-101,
 //                                                                      src/HashedNode.cpp:48-70
@@ -77,6 +78,16 @@ int ref_morton_keys(const double* pos3, size_t n, double size, uint64_t* keys) {
   for (size_t i = 0; i < n; ++i) {
     Vec3D p(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2]);
     keys[i] = computeMortonKey(p, size);
+  }
+  return 0;
+}
+
+int ref_decode_morton(const uint64_t* keys, size_t n, double size, double* pos3) {
+  for (size_t i = 0; i < n; ++i) {
+    const Vec3D p = decodeMortonKey(keys[i], size);
+    pos3[3 * i] = p.x;
+    pos3[3 * i + 1] = p.y;
+    pos3[3 * i + 2] = p.z;
   }
   return 0;
 }

@@ -41,7 +41,7 @@ EXPORTS = [
     "bh_step_backward", "bh_energy_diag", "bh_autotune_walk", "bh_set_walk_variant", "bh_plummer_device",
     "bh_batch_plummer_device", "bh_tree_boxes", "bh_save_snapshot", "bh_load_snapshot", "bh_get_stream",
     "bh_check_bounded_wait", "bh_solar_system_device", "bh_parse_horizons", "bh_step_host",
-    "bh_batch_step_host", "bh_set_stream",
+    "bh_batch_step_host", "bh_set_stream", "bh_decode_morton_keys",
 ]
 
 
@@ -162,6 +162,7 @@ def load():
         "bh_load_snapshot": ([P, ctypes.c_char_p], I),
         "bh_get_stream": ([P, ctypes.POINTER(P), ctypes.POINTER(I)], I),
         "bh_set_stream": ([P, P], I),
+        "bh_decode_morton_keys": ([P, P, S, D, P], I),
         "bh_check_bounded_wait": ([P, I, I], I),
         "bh_solar_system_device": ([P, ctypes.c_uint64, S, I], I),
         "bh_parse_horizons": ([ctypes.c_char_p, I, P, S, ctypes.POINTER(S)], I),
@@ -305,6 +306,14 @@ class Simulation:
         k = np.zeros(self.n, np.uint64)
         check(self.lib.bh_morton_keys(self.h, size, _ptr(k)), "bh_morton_keys")
         return k
+
+    def decode_morton_keys(self, keys, size):
+        """decodeMortonKey for each key (bh_decode_morton_keys): (n, 3) float64 positions."""
+        keys = np.ascontiguousarray(keys, np.uint64)
+        out = np.zeros((len(keys), 3))
+        check(self.lib.bh_decode_morton_keys(self.h, _ptr(keys), len(keys), size, _ptr(out)),
+              "bh_decode_morton_keys")
+        return out
 
     def sort_bodies(self):
         perm = np.zeros(self.n, np.uint32)

@@ -382,6 +382,26 @@ bh_status bh_morton_keys(bh_ctx* c, double size, uint64_t* keys_out) {
   return cuda_status(cudaStreamSynchronize(c->stream));
 }
 
+bh_status bh_decode_morton_keys(bh_ctx* c, const uint64_t* keys, size_t n, double size, double* pos3_out) {
+  if (!c || (n > 0 && (!keys || !pos3_out)) || n > (size_t)INT32_MAX) return BH_ERR_INVALID_ARG;
+  if (n == 0) return BH_OK;
+  cudaSetDevice(c->device);
+  uint64_t* dk = nullptr;
+  double* dp = nullptr;
+  BH_TRY(dalloc(&dk, n));
+  bh_status s = dalloc(&dp, 3 * n);
+  if (s == BH_OK) {
+    cudaMemcpyAsync(dk, keys, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, c->stream);
+    bh::launch_decode_morton(c, dk, (int)n, size, dp);
+    s = last_launch();
+    if (s == BH_OK) cudaMemcpyAsync(pos3_out, dp, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream);
+    if (s == BH_OK) s = cuda_status(cudaStreamSynchronize(c->stream));
+  }
+  dfree(dk);
+  dfree(dp);
+  return s;
+}
+
 bh_status bh_sort_bodies(bh_ctx* c, uint32_t* perm_out) {
   if (!c) return BH_ERR_INVALID_ARG;
   cudaSetDevice(c->device);

@@ -250,6 +250,7 @@ void walk_init();
 void launch_bounds(bh_ctx* c, const float4* pos, int n, double edge_factor);
 void launch_set_geom(bh_ctx* c, const double center[3], double size, const double tcenter[3], double tedge);
 void launch_morton(bh_ctx* c, const float4* pos, int n, uint64_t* keys, uint32_t* idx, bool batch = false);
+void launch_decode_morton(bh_ctx* c, const uint64_t* keys, int n, double size, double* pos3);
 void launch_gather(bh_ctx* c, const uint32_t* perm, int n, const float4* pin, const float4* vin, float4* pout,
                    float4* vout);
 void launch_gather_kd_treekey(bh_ctx* c, const uint32_t* perm, int n, const float4* pin, const float4* vin,

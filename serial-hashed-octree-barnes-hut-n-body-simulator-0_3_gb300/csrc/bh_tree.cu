@@ -301,6 +301,23 @@ __global__ __launch_bounds__(kThreads) void k_morton(const float4* __restrict__ 
   idx[i] = (uint32_t)i;
 }
 
+// decodeMortonKey (src/MortonKeys.hpp:204-228): each axis's 21 bits de-interleaved, then
+// x_int / 2^21 * 2 * S - S (the division and doubling are exact; one rounding each for the
+// product and the difference, as in the reference's FP64 expression).
+__global__ __launch_bounds__(kThreads) void k_decode_morton(const uint64_t* __restrict__ keys, int n, double S,
+                                                            double* __restrict__ pos3) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t k = keys[i];
+  uint32_t q[3] = {0u, 0u, 0u};
+#pragma unroll
+  for (int b = 0; b < kMaxDepth; ++b)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) q[a] |= (uint32_t)((k >> (3 * b + 2 - a)) & 1ull) << b;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) pos3[3 * i + a] = __dsub_rn(__dmul_rn((double)q[a] * 0x1p-20, S), S);
+}
+
 __global__ __launch_bounds__(kThreads) void k_treekey(const float4* __restrict__ pos, int n,
                                                       const Geom* __restrict__ g, uint64_t* __restrict__ tkeys,
                                                       uint32_t* __restrict__ tidx) {
@@ -1105,6 +1122,12 @@ void launch_morton(bh_ctx* c, const float4* pos, int n, uint64_t* keys, uint32_t
   if (n > 0)
     k_morton<<<grid_for(n), kThreads, 0, c->stream>>>(pos, n, batch ? c->sys_geom : c->geom,
                                                        batch ? c->body_sys : nullptr, keys, idx);
+}
+
+void launch_decode_morton(bh_ctx* c, const uint64_t* keys, int n, double size, double* pos3) {
+  if (n <= 0) return;
+  c->launches += 1;
+  k_decode_morton<<<grid_for(n), kThreads, 0, c->stream>>>(keys, n, size, pos3);
 }
 
 void launch_treekey(bh_ctx* c, const float4* pos, int n, uint64_t* tkeys, uint32_t* tidx) {

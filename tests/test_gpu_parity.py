@@ -376,3 +376,12 @@ def test_key_fast_paths_at_cell_boundaries(bh, orc, sim, S, center, edge):
     ref = orc.build(pos, mass, np.array(center), edge, 4, 1)
     assert np.array_equal(t["keys"], ref["keys"])
     assert np.array_equal(t["counts"], ref["counts"])
+
+
+def test_decode_morton_keys_bit_exact(bh, orc, sim):
+    """bh_decode_morton_keys against the oracle's decodeMortonKey restatement, bit for bit."""
+    rng = np.random.default_rng(9)
+    keys = np.concatenate([rng.integers(0, 2**63, 100000, dtype=np.uint64) | np.uint64(1 << 63),
+                           np.array([1 << 63, (1 << 64) - 1, 0], np.uint64)])
+    for size in (9.97, 1.0, 3.75e11):
+        assert np.array_equal(sim.decode_morton_keys(keys, size), orc.decode_morton(keys, size))

@@ -160,3 +160,18 @@ def test_intended_force_close_to_direct_sum(orc):
     assert np.median(err) < 1e-3
     lit, _, _ = orc.force(pos, mass, c, 2 * size, 1, 0, 0.5, 0.01, nthreads=4)
     assert np.median(relerr(lit, d)) > 1e-2  # the literal pseudo-barycentre walk is far less accurate
+
+
+def test_decode_morton_matches_reference(orc, ref):
+    """decodeMortonKey: the restatement equals the reference's own function bit for bit, on keys
+    of real positions and on arbitrary 64-bit words (the decode ignores bit 63 and reads every
+    axis bit)."""
+    rng = np.random.default_rng(8)
+    pos = rng.normal(0, 2, (5000, 3))
+    c, size = orc.bounds(pos)
+    keys = np.concatenate([orc.morton_keys(pos, size), rng.integers(0, 2**63, 3000, dtype=np.uint64) | (1 << 63)])
+    for s in (size, 1.0, 3.75e11):
+        assert np.array_equal(orc.decode_morton(keys, s), ref.decode_morton(keys, s))
+    # a key decodes to its cell's low corner: within one cell of the encoded position
+    dec = orc.decode_morton(keys[:5000], size)
+    assert np.all(np.abs(dec - pos) <= 2 * size / 2**21 * (1 + 1e-12))
