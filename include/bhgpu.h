@@ -265,13 +265,15 @@ bh_status bh_sort_keys_static(const uint64_t* keys_in, const uint32_t* vals_in, 
 
 /* Walk autotuner (no counterpart in the reference, whose walk is one serial loop). Times each
  * launch shape of the quadrupole tree walk (warps per block, register budget as resident blocks
- * per SM, per-warp stack depth; groups are always the 32 bodies of one warp, one per lane, since
- * the per-lane opening masks are 32-bit) on the tree currently in the context: the last
- * bh_step / bh_build, or the last bh_batch_step of an ensemble. Each shape runs `trials` timed
+ * per SM, per-warp stack depth, cell-evaluation form, and bodies per warp group: 32, or 16 / 8
+ * for a single system, where more and smaller groups fill the GPU at small N; a group never
+ * exceeds the 32 lanes of a warp, whose opening masks are 32-bit; ensembles walk their fixed
+ * table of groups of up to 32) on the tree currently in the context: the last bh_step /
+ * bh_build, or the last bh_batch_step of an ensemble. Each shape runs `trials` timed
  * force-only walks after one warm-up (the state is not changed); the fastest median becomes the
  * context's walk for quadrupole steps with eps > 0. Shapes whose stack cannot hold the tree get
  * ms = -1. */
-#define BH_TUNE_MAX_VARIANTS 8
+#define BH_TUNE_MAX_VARIANTS 12
 typedef struct bh_tune_result {
   int variants;
   int best;
@@ -280,6 +282,7 @@ typedef struct bh_tune_result {
   int stack_depth[BH_TUNE_MAX_VARIANTS];
   int cell_form[BH_TUNE_MAX_VARIANTS]; /* 0: three selects per cell; 1: one select on the common factor */
   int registers[BH_TUNE_MAX_VARIANTS];
+  int group_size[BH_TUNE_MAX_VARIANTS]; /* bodies per warp group */
   float ms[BH_TUNE_MAX_VARIANTS];
 } bh_tune_result;
 bh_status bh_autotune_walk(bh_ctx* ctx, double theta, double eps, int trials, bh_tune_result* out);

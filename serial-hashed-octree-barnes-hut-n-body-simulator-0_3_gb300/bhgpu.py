@@ -85,17 +85,23 @@ class Energy(ctypes.Structure):
                 for k, _ in self._fields_}
 
 
+TUNE_MAX_VARIANTS = 12  # BH_TUNE_MAX_VARIANTS
+
+
 class TuneResult(ctypes.Structure):
-    _fields_ = [("variants", ctypes.c_int), ("best", ctypes.c_int), ("warps_per_block", ctypes.c_int * 8),
-                ("min_blocks_per_sm", ctypes.c_int * 8), ("stack_depth", ctypes.c_int * 8),
-                ("cell_form", ctypes.c_int * 8), ("registers", ctypes.c_int * 8), ("ms", ctypes.c_float * 8)]
+    _fields_ = [("variants", ctypes.c_int), ("best", ctypes.c_int),
+                ("warps_per_block", ctypes.c_int * TUNE_MAX_VARIANTS),
+                ("min_blocks_per_sm", ctypes.c_int * TUNE_MAX_VARIANTS),
+                ("stack_depth", ctypes.c_int * TUNE_MAX_VARIANTS), ("cell_form", ctypes.c_int * TUNE_MAX_VARIANTS),
+                ("registers", ctypes.c_int * TUNE_MAX_VARIANTS), ("group_size", ctypes.c_int * TUNE_MAX_VARIANTS),
+                ("ms", ctypes.c_float * TUNE_MAX_VARIANTS)]
 
     def as_dict(self):
         k = self.variants
         return {"best": self.best,
                 "variants": [{"warps_per_block": self.warps_per_block[i], "min_blocks_per_sm": self.min_blocks_per_sm[i],
                               "stack_depth": self.stack_depth[i], "cell_form": self.cell_form[i],
-                              "registers": self.registers[i], "ms": self.ms[i]}
+                              "registers": self.registers[i], "group_size": self.group_size[i], "ms": self.ms[i]}
                              for i in range(k)]}
 
 

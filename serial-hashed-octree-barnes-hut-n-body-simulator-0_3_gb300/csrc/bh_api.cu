@@ -1204,6 +1204,7 @@ bh_status bh_autotune_walk(bh_ctx* c, double theta, double eps, int trials, bh_t
     out->stack_depth[v] = info.stack;
     out->cell_form[v] = info.form;
     out->registers[v] = info.regs;
+    out->group_size[v] = batch ? 32 : info.group;  // ensembles walk their fixed group table
     std::vector<float> ms;
     uint32_t e = 0;
     for (int t = 0; t <= trials && e == 0; ++t) {  // trial 0 warms up

@@ -274,7 +274,7 @@ void launch_walk_record(bh_ctx* c, int n, float theta, float eps, float4* acc_sl
 void launch_fp32_peak(cudaStream_t st, float* sink, int blocks);
 // Launch shapes of the quadrupole walk (positive softening) that bh_autotune_walk times.
 struct WalkVariant {
-  int warps, min_blocks, stack, form, regs;
+  int warps, min_blocks, stack, form, regs, group;  // group: bodies per warp (single systems)
 };
 int walk_variants();
 WalkVariant walk_variant_info(int v);

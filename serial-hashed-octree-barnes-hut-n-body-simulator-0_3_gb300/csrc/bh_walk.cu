@@ -1,6 +1,7 @@
 // Tree walk + force: ComputeHOTOctreeForce / TraverseHOTInteractionList /
 // ComputeHOTForceInteractionList / LinearHashedOctree::MAC (src/HashedOctree.hpp:262-459,
-// src/HashedOctree.cpp:872-885), one warp per group of 32 consecutive bodies in tree order.
+// src/HashedOctree.cpp:872-885), one warp per group of up to 32 consecutive bodies in tree order
+// (32 by default; the autotuner may pick 16 or 8 for small single systems).
 //
 // Per-lane exactness. The reference walks each body separately: pop a node; test each
 // existing child with the MAC size^2 / d^2 < theta^2 against the body; accepted children go
@@ -238,7 +239,7 @@ __global__ __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) void k_walk(const W
                                                    const uint32_t* __restrict__ tslot, int n, float theta2,
                                                    float eps2, float4* __restrict__ acc_slot,
                                                    float4* __restrict__ vel_kick, float half_dt,
-                                                   const int4* __restrict__ groups, int ngroups_table,
+                                                   const int4* __restrict__ groups, int ngroups_table, int gsize,
                                                    Counters* __restrict__ ctr, uint32_t* __restrict__ err,
                                                    Chunk* __restrict__ tape = nullptr,
                                                    unsigned* __restrict__ tape_count = nullptr, int tape_cap = 0) {
@@ -250,9 +251,10 @@ __global__ __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) void k_walk(const W
   WarpSmemT<kStack>& s = smem[threadIdx.x >> 5];
   if (*((volatile uint32_t*)err) & (kErrNodes | kErrTimeout)) return;
   // work items: groups of up to 32 consecutive bodies (tree order) under one root. Without a
-  // group table, group g is bodies [32 g, 32 g + 32) of the single tree rooted at node 0;
-  // batched ensembles pass (first body, body count, root node) per group.
-  const int ngroups = groups ? ngroups_table : (n + 31) >> 5;
+  // group table, group g is bodies [gsize g, gsize g + gsize) of the single tree rooted at node 0
+  // (gsize <= 32; lanes beyond the group's bodies stay out of every mask); batched ensembles pass
+  // (first body, body count, root node) per group.
+  const int ngroups = groups ? ngroups_table : (n + gsize - 1) / gsize;
   const float acc_scale = theta2 * (1.f - kMacMargin);
   const float open_scale = theta2 * (1.f + kMacMargin);
   unsigned long long tot_cell = 0, tot_pt = 0, ev_cell = 0, ev_pt = 0;  // ev_*: warp-uniform
@@ -270,8 +272,8 @@ __global__ __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) void k_walk(const W
       gcount = gr.y;
       root = gr.z;
     } else {
-      gbase = g * 32;
-      gcount = min(32, n - gbase);
+      gbase = g * gsize;
+      gcount = min(gsize, n - gbase);
       root = 0;
     }
     const int4 root_link = __ldg(&nodes[root].link);
@@ -561,12 +563,12 @@ int walk_grid() {
 
 template <bool kQuad, bool kSelf, class Cfg = CfgDefault>
 void launch_walk_t(bh_ctx* c, int n, float theta2, float eps2, float4* acc_slot, float4* vel_kick, float half_dt,
-                   bool batch) {
-  const int ngroups = batch ? c->ngroups : (n + 31) / 32;
+                   bool batch, int gsize = 32) {
+  const int ngroups = batch ? c->ngroups : (n + gsize - 1) / gsize;
   const int grid = min(walk_grid<kQuad, kSelf, false, Cfg>(), ngroups / Cfg::kWarps + 1);
   k_walk<kQuad, kSelf, false, Cfg><<<grid, Cfg::kThreads, 0, c->stream>>>(
       c->wnode, c->tpos, c->tslot, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch ? c->groups : nullptr,
-      c->ngroups, c->counters, c->err);
+      c->ngroups, gsize, c->counters, c->err);
 }
 
 // Launch shapes the autotuner chooses from for the quadrupole walk with positive softening
@@ -579,13 +581,15 @@ using Cfg4 = WalkCfg<4, 6, 384>;
 using Cfg5 = WalkCfg<4, 8, 512>;
 using Cfg6 = WalkCfg<8, 4, 384, 1>;
 using Cfg7 = WalkCfg<4, 8, 384, 1>;
-constexpr int kVariants = 8;
+// variants 8 and 9: the default shape with groups of 16 and 8 bodies (single systems; more,
+// smaller groups fill the GPU when N is small)
+constexpr int kVariants = 10;
 
 template <class Cfg>
-WalkVariant variant_info() {
+WalkVariant variant_info(int group = 32) {
   cudaFuncAttributes fa{};
   cudaFuncGetAttributes(&fa, k_walk<true, false, false, Cfg>);
-  return {Cfg::kWarps, Cfg::kMinBlocks, Cfg::kStack, Cfg::kForm, fa.numRegs};
+  return {Cfg::kWarps, Cfg::kMinBlocks, Cfg::kStack, Cfg::kForm, fa.numRegs, group};
 }
 
 void launch_quad_variant(bh_ctx* c, int v, int n, float theta2, float eps2, float4* acc_slot, float4* vel_kick,
@@ -598,6 +602,8 @@ void launch_quad_variant(bh_ctx* c, int v, int n, float theta2, float eps2, floa
     case 5: launch_walk_t<true, false, Cfg5>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
     case 6: launch_walk_t<true, false, Cfg6>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
     case 7: launch_walk_t<true, false, Cfg7>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
+    case 8: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, 16); break;
+    case 9: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, 8); break;
     default: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
   }
 }
@@ -615,6 +621,8 @@ WalkVariant walk_variant_info(int v) {
     case 5: return variant_info<Cfg5>();
     case 6: return variant_info<Cfg6>();
     case 7: return variant_info<Cfg7>();
+    case 8: return variant_info<CfgDefault>(16);
+    case 9: return variant_info<CfgDefault>(8);
     default: return variant_info<CfgDefault>();
   }
 }
@@ -679,7 +687,7 @@ void launch_walk_record(bh_ctx* c, int n, float theta, float eps, float4* acc_sl
   const int grid = min(walk_grid<true, false, true, CfgDefault>(), ((n + 31) / 32) / kWarps + 1);
   k_walk<true, false, true><<<grid, kThreads, 0, c->stream>>>(c->wnode, c->tpos, c->tslot, n, theta * theta,
                                                               eps * eps, acc_slot, vel_kick, half_dt, nullptr, 0,
-                                                              c->counters, c->err, tape, tape_count, tape_cap);
+                                                              32, c->counters, c->err, tape, tape_count, tape_cap);
 }
 
 }  // namespace bh

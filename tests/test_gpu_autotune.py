@@ -55,9 +55,9 @@ def test_autotune_batched_then_step(bh):
     assert float(np.median(relerr(out[0][2], out[1][2]))) < 1e-5
 
 
-@pytest.mark.parametrize("variant", range(8))
+@pytest.mark.parametrize("variant", range(10))
 def test_every_walk_variant_matches_oracle(bh, orc, variant):
-    """Each launch shape (and cell-evaluation form) the tuner can pick gives the reference's
+    """Each launch shape (cell-evaluation form, group size) the tuner can pick gives the reference's
     interaction sets and accelerations within the parity bars."""
     n = 20000
     pm, vel = bh.plummer(9, n)
