@@ -86,6 +86,21 @@ class Dist:
             td.init_process_group("gloo")
             self.td = td
 
+    def device(self):
+        """This rank's GPU: the local rank under torchrun (one replica per GPU), else 0."""
+        return self.local if self.ws > 1 else 0
+
+    def simulation(self, bh, n):
+        """A context on this rank's GPU (device 0 when the rank's GPU is the only visible one)."""
+        try:
+            return bh.Simulation(n, device=self.device())
+        except bh.BHError:
+            return bh.Simulation(n, device=0)
+
+    def gpu_index(self):
+        """nvidia-smi index of this rank's GPU (BH_GPU_INDEX overrides)."""
+        return int(os.environ.get("BH_GPU_INDEX", str(self.device())))
+
     def barrier(self):
         if self.ws > 1:
             self.td.barrier()
@@ -313,7 +328,7 @@ def run_ours(args, w, dist):
     pm, vel = make_inputs(bh, w, w["seed"] + dist.rank)
     prm = bh.default_params(theta=w["theta"], eps=w["eps"], dt=w["dt"], leaf_capacity=w["leaf"],
                             multipole=bh.BH_MULTIPOLE_QUADRUPOLE, edge_factor=w["edge"], acc_follows_body=1)
-    sim = bh.Simulation(n, device=0)
+    sim = dist.simulation(bh, n)
     sim.set_bodies(pm, vel)
 
     # step-0 accelerations for the accuracy gate (rank 0, before stepping)
@@ -337,7 +352,7 @@ def run_ours(args, w, dist):
     sim.synchronize()
     energy0 = sim.energy(w["theta"], w["eps"])  # over the tree of the last warm-up step
 
-    gpu_index = int(os.environ.get("BH_GPU_INDEX", "0"))
+    gpu_index = dist.gpu_index()
     per_step_ms, walk_ms, sort_ms, flops, inter, util_cell, util_pt = [], [], [], [], [], [], []
     stage = {}
     launches = 0
@@ -488,7 +503,7 @@ def run_ensemble(args, dist):
     n = int(off[-1])
     prm = bh.default_params(theta=e["theta"], eps=e["eps"], dt=e["dt"], leaf_capacity=e["leaf"],
                             multipole=bh.BH_MULTIPOLE_QUADRUPOLE, edge_factor=e["edge"], acc_follows_body=1)
-    sim = bh.Simulation(n)
+    sim = dist.simulation(bh, n)
     # the ensemble's initial conditions come from the device generator (system s: seed + s)
     sim.batch_plummer_device(e["seed"], off)
     pos, vel, _ = sim.get_bodies()
@@ -500,7 +515,7 @@ def run_ensemble(args, dist):
     per_step, flops = [], []
     launches = 0
     dist.barrier()
-    with ClockSampler(int(os.environ.get("BH_GPU_INDEX", "0"))) as clocks:
+    with ClockSampler(dist.gpu_index()) as clocks:
         for _ in range(args.steps):
             sim.flush_l2()
             st = sim.batch_step(prm, 1)
@@ -533,7 +548,7 @@ def run_ensemble(args, dist):
     loop_s = []
     for s in sample:
         a, b = int(off[s]), int(off[s + 1])
-        with bh.Simulation(b - a) as one:
+        with dist.simulation(bh, b - a) as one:
             one.set_bodies(pos[a:b], vel[a:b])
             for _ in range(2):
                 one.step(prm, 1, stats=False)
@@ -599,7 +614,7 @@ def run_adjoint(args, dist):
     pm, vel = bh.plummer(a["seed"], n)
     prm = bh.default_params(theta=a["theta"], eps=a["eps"], dt=a["dt"], leaf_capacity=a["leaf"],
                             multipole=bh.BH_MULTIPOLE_QUADRUPOLE, edge_factor=a["edge"], acc_follows_body=1)
-    sim = bh.Simulation(n)
+    sim = dist.simulation(bh, n)
     tpm = pm.copy()
     tpm[:, 3] *= np.random.default_rng(a["tseed"]).lognormal(0.0, 0.1, n).astype(np.float32)
     sim.set_bodies(tpm, vel)
@@ -622,7 +637,7 @@ def run_adjoint(args, dist):
         gradient(False)
     fwd, bwd, launches = [], [], 0
     dist.barrier()
-    with ClockSampler(int(os.environ.get("BH_GPU_INDEX", "0"))) as clocks:
+    with ClockSampler(dist.gpu_index()) as clocks:
         for _ in range(args.steps):
             f, b, loss = gradient(True)
             fwd.append(f.ms_step)
