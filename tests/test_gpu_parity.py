@@ -385,3 +385,56 @@ def test_decode_morton_keys_bit_exact(bh, orc, sim):
                            np.array([1 << 63, (1 << 64) - 1, 0], np.uint64)])
     for size in (9.97, 1.0, 3.75e11):
         assert np.array_equal(sim.decode_morton_keys(keys, size), orc.decode_morton(keys, size))
+
+
+def test_full_size_two_spheres(bh, orc):
+    """Config 2 at full size (two Plummer spheres of 2^21, the deep-tree stress case): keys,
+    permutation, node-key set and node counts bit-exact at leaf 8, and forces on a seeded
+    subsample within the parity bars (theta 0.5, softening 0.001)."""
+    n = 1 << 22
+    pm, v = bh.two_spheres(0, n)
+    pos = pm[:, :3].astype(np.float64)
+    with bh.Simulation(n) as s:
+        s.set_bodies(pm, v)
+        c, size = s.bounds()
+        keys = s.morton_keys(size)
+        assert np.array_equal(keys, orc.morton_keys(pos, size))
+        perm = s.sort_bodies()
+        assert np.array_equal(perm, orc.sort_perm(keys))
+        sp = pm[perm]
+        p2, m2 = sp[:, :3].astype(np.float64), sp[:, 3].astype(np.float64)
+        s.build(c, 2 * size, 8, bh.BH_MULTIPOLE_QUADRUPOLE)
+        t = s.tree_nodes()
+        ref_t = orc.build(p2, m2, c, 2 * size, 8, 1)
+        assert np.array_equal(t["keys"], ref_t["keys"])
+        assert np.array_equal(t["counts"], ref_t["counts"])
+        assert (int(t["keys"][-1]).bit_length() - 1) // 3 >= 12  # the deepest level (14 here)
+        acc = s.force(0.5, 0.001)
+        tgt = np.random.default_rng(2).choice(n, 4096, replace=False).astype(np.uint32)
+        ref_acc, _, _ = orc.force(p2, m2, c, 2 * size, 8, 1, 0.5, 0.001, targets=tgt, nthreads=16)
+        assert_acc_close(acc[tgt], ref_acc)
+
+
+def test_full_size_step_properties(bh):
+    """Size-independent properties at N = 2^22: through fused steps the body ids riding in the
+    velocity lane stay a permutation of 0..N-1 and the total mass is kept; a sort orders the
+    keys and a second sort of the same keys is the identity."""
+    n = 1 << 22
+    pm, v = bh.plummer(3, n)
+    v[:, 3] = np.arange(n, dtype=np.float32)
+    prm = bh.default_params(theta=0.5, eps=0.005, dt=5e-4, leaf_capacity=16, multipole=1, edge_factor=2.0)
+    with bh.Simulation(n) as s:
+        s.set_bodies(pm, v)
+        for _ in range(2):
+            s.step(prm, 1)
+            p, vv, _ = s.get_bodies()
+            assert np.array_equal(np.sort(vv[:, 3].astype(np.int64)), np.arange(n))
+            assert abs(float(p[:, 3].astype(np.float64).sum()) - float(pm[:, 3].astype(np.float64).sum())) < 1e-6
+        # the drifted positions' keys: sorting orders them, and sorting again is the identity
+        c, size = s.bounds()
+        s.morton_keys(size)
+        s.sort_bodies()
+        again = s.sort_bodies()
+        assert np.array_equal(again, np.arange(n, dtype=again.dtype))
+        keys = s.morton_keys(size)
+        assert np.all(keys[1:] >= keys[:-1])
