@@ -111,3 +111,36 @@ def test_batch_step_host_matches_batch_step(bh):
     finally:
         for x in bufs:
             x.free()
+
+
+def test_batch_at_the_system_limit(bh):
+    """65 535 systems (the most the 16-bit system ids allow) of 1 to 4 bodies: the ensemble steps,
+    sampled systems match their own plain steps, and one more system is refused."""
+    rng = np.random.default_rng(11)
+    nsys = 65535
+    sizes = rng.integers(1, 5, nsys)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint32)
+    n = int(off[-1])
+    pm = np.zeros((n, 4), np.float32)
+    pm[:, :3] = rng.normal(0, 1, (n, 3)).astype(np.float32)
+    pm[:, 3] = 0.25
+    vel = np.zeros((n, 4), np.float32)
+    vel[:, :3] = rng.normal(0, 0.1, (n, 3)).astype(np.float32)
+    vel[:, 3] = np.arange(n, dtype=np.float32)
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=1, multipole=1, edge_factor=2.0)
+    with bh.Simulation(n + 8) as sim:
+        sim.batch_set(pm, vel, off)
+        st = sim.batch_step(prm, 2)
+        assert st.steps == 2 and st.error_flags == 0
+        bp, bv, _ = sim.get_bodies()
+        with pytest.raises(bh.BHError):
+            sim.batch_set(np.concatenate([pm, pm[:1]]), np.concatenate([vel, vel[:1]]),
+                          np.concatenate([off, [n + 1]]).astype(np.uint32))
+    with bh.Simulation(8) as one:
+        for s in list(rng.choice(nsys, 20, replace=False)) + [nsys - 1]:
+            a, b = off[s], off[s + 1]
+            one.set_bodies(pm[a:b], vel[a:b])
+            one.step(prm, 2)
+            p, v, _ = one.get_bodies()
+            assert np.array_equal(bv[a:b, 3], v[:, 3])
+            assert np.allclose(bp[a:b, :3], p[:, :3], rtol=0, atol=1e-6)
