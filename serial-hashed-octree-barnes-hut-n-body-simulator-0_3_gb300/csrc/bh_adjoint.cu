@@ -71,6 +71,7 @@ struct AdjState {
   unsigned* next = nullptr;
   bool valid = false;
   bool vjp_attr = false;
+  int vjp_blocks_per_sm = 0;  // resident k_vjp blocks per SM (queried once)
 };
 
 __global__ void k_adj_abar(const float4* __restrict__ vbar, const float4* __restrict__ carry, float h, int n,
@@ -95,12 +96,33 @@ __global__ void k_adj_vupdate(float4* __restrict__ vbar, const float4* __restric
 }
 
 // Per-warp shared memory of the replay: the group's bodies and their acceleration adjoints, and
-// the 32 x 32 table (padded rows, conflict-free both ways) of body-side terms for each axis.
+// a 16 x 32 table (padded rows, conflict-free both ways) of body-side terms for each axis: the
+// bodies are taken 16 at a time, which halves the table and doubles the resident warps.
+constexpr int kVjpHalf = 16;
 struct VjpWarp {
   float4 pos[32];
   float4 ab[32];
-  float g[3][32][33];
+  float g[3][kVjpHalf][33];
 };
+
+// Lane b of the half [h, h + 16) sums its body's row over the chunk's entries; d = source -
+// body, so the body's own position takes the negative.
+__device__ __forceinline__ void vjp_rows(VjpWarp& s, int h, int hend, int lane, int cnt, uint32_t my_slot,
+                                         float4* __restrict__ xbar) {
+  __syncwarp();
+  if (lane >= h && lane < hend) {
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int k = 0; k < cnt; ++k) {
+      sx += s.g[0][lane - h][k];
+      sy += s.g[1][lane - h][k];
+      sz += s.g[2][lane - h][k];
+    }
+    atomicAdd(&xbar[my_slot].x, -sx);
+    atomicAdd(&xbar[my_slot].y, -sy);
+    atomicAdd(&xbar[my_slot].z, -sz);
+  }
+  __syncwarp();
+}
 
 constexpr int kVjpWarps = 4;
 constexpr size_t kVjpSmem = sizeof(VjpWarp) * kVjpWarps;
@@ -142,7 +164,9 @@ __global__ __launch_bounds__(kVjpWarps * 32) void k_vjp(const Chunk* __restrict_
       const float M = B.x, qxx = B.y, qxy = B.z, qxz = B.w, qyy = Q2.x, qyz = Q2.y, qzz = Q2.z;
       float cbx = 0.f, cby = 0.f, cbz = 0.f, mb = 0.f;
       float bxx = 0.f, bxy = 0.f, bxz = 0.f, byy = 0.f, byz = 0.f, bzz = 0.f;
-      for (int b = 0; b < gcount; ++b) {
+      for (int h = 0; h < gcount; h += kVjpHalf) {
+      const int hend = min(h + kVjpHalf, gcount);
+      for (int b = h; b < hend; ++b) {
         const float4 p = s.pos[b], ab = s.ab[b];
         const bool take = (mk >> b) & 1u;
         const float dx = C.x - p.x, dy = C.y - p.y, dz = C.z - p.z;
@@ -166,9 +190,9 @@ __global__ __launch_bounds__(kVjpWarps * 32) void k_vjp(const Chunk* __restrict_
         const float gx = fmaf(ca, ab.x, fmaf(cd, dx, fmaf(cq, Qdx, -w5t * Qax)));
         const float gy = fmaf(ca, ab.y, fmaf(cd, dy, fmaf(cq, Qdy, -w5t * Qay)));
         const float gz = fmaf(ca, ab.z, fmaf(cd, dz, fmaf(cq, Qdz, -w5t * Qaz)));
-        s.g[0][b][lane] = gx;
-        s.g[1][b][lane] = gy;
-        s.g[2][b][lane] = gz;
+        s.g[0][b - h][lane] = gx;
+        s.g[1][b - h][lane] = gy;
+        s.g[2][b - h][lane] = gz;
         cbx += gx;
         cby += gy;
         cbz += gz;
@@ -181,6 +205,8 @@ __global__ __launch_bounds__(kVjpWarps * 32) void k_vjp(const Chunk* __restrict_
         bxy += fmaf(-w5, fmaf(ax, dy, ay * dx), 2.f * h25 * dx * dy);
         bxz += fmaf(-w5, fmaf(ax, dz, az * dx), 2.f * h25 * dx * dz);
         byz += fmaf(-w5, fmaf(ay, dz, az * dy), 2.f * h25 * dy * dz);
+      }
+      vjp_rows(s, h, hend, lane, cnt, my_slot, xbar);
       }
       if (has && mk) {
         float* a = nadj + (size_t)e * kNadj;
@@ -199,7 +225,9 @@ __global__ __launch_bounds__(kVjpWarps * 32) void k_vjp(const Chunk* __restrict_
       const int src = has ? (e >= 0 ? e : nodes[-e - 1].link.z) : 0;  // a point node is a single-body leaf
       const float4 v = tpos[src];
       float tx = 0.f, ty = 0.f, tz = 0.f, tm = 0.f;
-      for (int b = 0; b < gcount; ++b) {
+      for (int h = 0; h < gcount; h += kVjpHalf) {
+      const int hend = min(h + kVjpHalf, gcount);
+      for (int b = h; b < hend; ++b) {
         const float4 p = s.pos[b], ab = s.ab[b];
         const bool take = ((mk >> b) & 1u) && src != gbase + b;
         const float dx = v.x - p.x, dy = v.y - p.y, dz = v.z - p.z;
@@ -212,13 +240,15 @@ __global__ __launch_bounds__(kVjpWarps * 32) void k_vjp(const Chunk* __restrict_
         const float gx = v.w * fmaf(w3, ab.x, k3 * dx);
         const float gy = v.w * fmaf(w3, ab.y, k3 * dy);
         const float gz = v.w * fmaf(w3, ab.z, k3 * dz);
-        s.g[0][b][lane] = gx;
-        s.g[1][b][lane] = gy;
-        s.g[2][b][lane] = gz;
+        s.g[0][b - h][lane] = gx;
+        s.g[1][b - h][lane] = gy;
+        s.g[2][b - h][lane] = gz;
         tx += gx;
         ty += gy;
         tz += gz;
         tm = fmaf(w3, ad, tm);
+      }
+      vjp_rows(s, h, hend, lane, cnt, my_slot, xbar);
       }
       if (has && mk) {
         const uint32_t ss = tslot[src];
@@ -227,19 +257,6 @@ __global__ __launch_bounds__(kVjpWarps * 32) void k_vjp(const Chunk* __restrict_
         atomicAdd(&xbar[ss].z, tz);
         atomicAdd(&mbar[ss], tm);
       }
-    }
-    __syncwarp();
-    if (lane < gcount) {
-      float sx = 0.f, sy = 0.f, sz = 0.f;
-      for (int k = 0; k < cnt; ++k) {
-        sx += s.g[0][lane][k];
-        sy += s.g[1][lane][k];
-        sz += s.g[2][lane][k];
-      }
-      // d = source - body, so the body's own position takes the negative
-      atomicAdd(&xbar[my_slot].x, -sx);
-      atomicAdd(&xbar[my_slot].y, -sy);
-      atomicAdd(&xbar[my_slot].z, -sz);
     }
   }
 }
@@ -452,10 +469,13 @@ bh_status vjp(bh_ctx* c, AdjState* a, const TapeSlot& t) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (!a->vjp_attr) {
     BH_TRY(cuda_status(cudaFuncSetAttribute(k_vjp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVjpSmem)));
+    int per_sm = 0;
+    BH_TRY(cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_vjp, kVjpWarps * 32, kVjpSmem)));
+    a->vjp_blocks_per_sm = std::max(1, per_sm);
     a->vjp_attr = true;
   }
-  // four resident blocks of four warps per SM (55 KB of shared memory each)
-  const int grid = std::max(1, std::min(sms * 4, (int)(t.nchunks / kVjpWarps) + 1));
+  // every resident block of four warps (30 KB of shared memory each)
+  const int grid = std::max(1, std::min(sms * a->vjp_blocks_per_sm, (int)(t.nchunks / kVjpWarps) + 1));
   const float eps2 = (float)(a->prm.eps * a->prm.eps);
   c->launches += 2;
   if (t.nchunks > 0)
