@@ -512,7 +512,8 @@ def run_ensemble(args, dist):
     tune = sim.autotune(e["theta"], e["eps"], trials=2)  # walk launch shape for this ensemble
     for _ in range(args.warmup - 1):  # re-captures the step graph with the chosen walk
         sim.batch_step(prm, 1, stats=False)
-    per_step, flops = [], []
+    per_step, flops, walk_ms = [], [], []
+    stage = {}
     launches = 0
     dist.barrier()
     with ClockSampler(dist.gpu_index()) as clocks:
@@ -521,7 +522,11 @@ def run_ensemble(args, dist):
             st = sim.batch_step(prm, 1)
             launches += st.kernel_launches
             per_step.append(st.ms_step)
+            walk_ms.append(st.ms_walk)
             flops.append(FLOPS_P2P * st.interactions_p2p + FLOPS_CELL_QUAD * st.interactions_cell)
+            for key, val in st.as_dict().items():
+                if key.startswith("ms_"):
+                    stage[key] = stage.get(key, 0.0) + val
     total_ms = dist.max(sum(per_step))
     value = dist.sum(n * args.steps) / (total_ms * 1e-3)
     # end to end: bh_batch_step_host uploads every system's positions and velocities from pinned
@@ -560,6 +565,7 @@ def run_ensemble(args, dist):
             loop_s.append(statistics.median(t))
     loop_step_s = sum(loop_s) * e["nsys"] / len(sample)
     walk_tflops = statistics.mean(flops) / (statistics.mean(per_step) * 1e-3) / 1e12
+    walk_only_tflops = statistics.mean(flops) / (statistics.mean(walk_ms) * 1e-3) / 1e12 if min(walk_ms) > 0 else None
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         # the oracle port on one core over 12 seeded systems, scaled by sum N log N
@@ -578,7 +584,7 @@ def run_ensemble(args, dist):
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "ours",
                 "config": {"workload": "ensemble-4096", "systems": e["nsys"], "bodies": n, "desc": e["desc"],
-                           "timing": "per-step CUDA events around the graph launch; L2 flushed between steps"},
+                           "timing": "per-step CUDA events inside the captured step; L2 flushed between steps"},
                 "e2e": {"value": n / (statistics.median(e2e) * 1e-3), "unit": "body-steps/s",
                         "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
                         "ms_per_step": statistics.median(e2e)},
@@ -588,6 +594,13 @@ def run_ensemble(args, dist):
                 "batched_speedup_vs_plain_loop": loop_step_s / (total_ms / args.steps * 1e-3),
                 "flops_per_step": statistics.mean(flops), "tflops": walk_tflops,
                 "fp32_peak_tflops": fp32_peak, "gpu_launches": launches, "autotune": tune,
+                "roofline": {"kernel": "k_walk<quadrupole> (ensemble groups)", "bound": "fp32",
+                             "achieved": walk_only_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                             "frac": (walk_only_tflops / fp32_peak) if walk_only_tflops and fp32_peak else None,
+                             "peak_source": "measured FP32 FMA peak of this GPU (bh_measure_fp32_peak)",
+                             "traffic": None, "flops_per_launch": statistics.mean(flops),
+                             "ms_per_launch": statistics.mean(walk_ms)},
+                "stage_ms_per_step": {k[3:]: v / args.steps for k, v in stage.items()},
                 "clocks": clocks.summary()}
         if cpu:
             line["cpu_baseline"] = cpu

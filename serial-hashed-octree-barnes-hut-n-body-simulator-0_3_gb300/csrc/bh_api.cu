@@ -940,18 +940,25 @@ void enqueue_batch_step(bh_ctx* c, const bh_params& p, const HostIO* io) {
     cudaEventRecord(c->io_ev[1], c->copy_stream);
     if (io->pos_in) cudaMemcpyAsync(c->pos[cur], io->pos_in, bytes, cudaMemcpyHostToDevice, c->stream);
   }
+  // stage events as in the plain step (external event-record nodes in the captured graph)
+  auto mark = [&](int k) { cudaEventRecordWithFlags(c->stage_ev[k], c->stream, cudaEventRecordExternal); };
   clear_device_flags(c);
+  mark(0);
   bh::launch_batch_bounds(c, c->pos[c->cur], p.edge_factor);
+  mark(1);
   bh::launch_morton(c, c->pos[c->cur], n, c->keys[0], c->vals[0], true);
+  mark(2);
   uint64_t* ko;
   uint32_t* vo;
   bh::radix_sort_pairs(c, c->keys[0], c->vals[0], c->keys[1], c->vals[1], n, c->stream, &ko, &vo);
   bh::launch_sys_keys(c, c->vals[0], n, c->keys[1]);
   bh::radix_sort_pairs(c, c->keys[1], c->vals[0], c->keys[0], c->vals[1], n, c->stream, &ko, &vo, 0, 2);
+  mark(3);
   // vals[0]: (system, Morton key) order; keys[0] receives the per-slot tree keys
   if (io) cudaStreamWaitEvent(c->stream, c->io_ev[1], 0);
   bh::launch_gather_kd_treekey(c, c->vals[0], n, c->pos[cur], c->vel[cur], c->acc, p.acc_follows_body, dt,
                                c->pos[nx], c->vel[nx], c->keys[0], c->tslot, true);
+  mark(4);
   if (io) {
     cudaEventRecord(c->io_ev[2], c->stream);
     cudaStreamWaitEvent(c->copy_stream, c->io_ev[2], 0);
@@ -963,9 +970,13 @@ void enqueue_batch_step(bh_ctx* c, const bh_params& p, const HostIO* io) {
   bh::launch_sys_keys(c, c->tslot, n, c->keys[1]);
   bh::radix_sort_pairs(c, c->keys[1], c->tslot, c->tkey, c->vals[1], n, c->stream, &ko, &vo, 0, 2);
   bh::launch_gather_tree_keys(c, c->tslot, n, c->pos[nx], c->keys[0], c->tpos, c->tkey);
+  mark(5);
   bh::launch_build(c, n, p.leaf_capacity, true);
+  mark(6);
   bh::launch_upsweep(c, n, p.leaf_capacity, p.multipole, true);
+  mark(7);
   bh::launch_walk(c, n, (float)p.theta, (float)p.eps, p.multipole, c->acc, c->vel[nx], 0.5f * dt, true);
+  mark(8);
   if (io) {
     if (io->vel_out) cudaMemcpyAsync(io->vel_out, c->vel[nx], bytes, cudaMemcpyDeviceToHost, c->stream);
     cudaStreamWaitEvent(c->stream, c->io_ev[3], 0);  // join
@@ -1108,10 +1119,8 @@ bh_status run_batch_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats*
           c->host_graph_ptrs[par][3] = io->vel_out;
         }
       }
-      if (st) cudaEventRecord(c->stage_ev[0], c->stream);
       BH_TRY(cuda_status(cudaGraphLaunch(graph, c->stream)));
       c->launches += kernels;
-      if (st) cudaEventRecord(c->stage_ev[1], c->stream);
       BH_TRY(sync_and_check(c, &e));
       if (e & bh::kErrNodes) {  // arena too small: grow it, re-capture, redo the step
         destroy_graphs(c);
@@ -1124,7 +1133,15 @@ bh_status run_batch_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats*
     if (e) return err_to_status(e);
     c->cur = 1 - c->cur;
     if (st) {
-      st->ms_step += elapsed(c, 0, 1);
+      st->ms_step += elapsed(c, 0, 8);
+      st->ms_bounds += elapsed(c, 0, 1);
+      st->ms_morton += elapsed(c, 1, 2);
+      st->ms_sort += elapsed(c, 2, 3);
+      st->ms_kick_drift += elapsed(c, 3, 4);
+      st->ms_sort_tree += elapsed(c, 4, 5);
+      st->ms_build += elapsed(c, 5, 6);
+      st->ms_upsweep += elapsed(c, 6, 7);
+      st->ms_walk += elapsed(c, 7, 8);
       st->n_nodes = (uint64_t)c->h_level_bounds[kLevels];
       st->interactions_cell += c->h_counters->cell;
       st->interactions_p2p += c->h_counters->p2p;
