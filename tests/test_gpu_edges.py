@@ -208,3 +208,19 @@ def test_caller_stream(bh):
         got = b.get_bodies()
     for g, r in zip(got, ref):
         assert np.array_equal(g, r)
+    # the host-copy step on the caller's stream (its copies still fork to the second stream)
+    bufs = [bh.PinnedArray((n, 4)) for _ in range(4)]
+    try:
+        with bh.Simulation(n) as c:
+            c.set_bodies(pm, vel)
+            assert lib.bh_set_stream(c.h, ctypes.c_void_p(user.cuda_stream)) == 0
+            p, v = pm.copy(), vel.copy()
+            for _ in range(4):
+                bufs[0].array[:] = p
+                bufs[1].array[:] = v
+                c.step_host(prm, bufs[0].array, bufs[1].array, bufs[2].array, bufs[3].array)
+                p, v = bufs[2].array.copy(), bufs[3].array.copy()
+        assert np.array_equal(p, ref[0]) and np.array_equal(v, ref[1])
+    finally:
+        for x in bufs:
+            x.free()
