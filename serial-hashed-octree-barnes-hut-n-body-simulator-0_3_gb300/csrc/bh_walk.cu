@@ -207,11 +207,12 @@ __device__ __forceinline__ void eval_points(Smem& s, int cnt, const WalkNode* __
     const float mr3 = v.w * rinv * rinv * rinv;
     bool take = (mk & lanebit) != 0u;
     if (kSelfTest) take = take && !((dx == 0.f) & (dy == 0.f) & (dz == 0.f));
-    if (take) {
-      bx = fmaf(mr3, dx, bx);
-      by = fmaf(mr3, dy, by);
-      bz = fmaf(mr3, dz, bz);
-    }
+    // a select, not a branch (walk 17.38 -> 17.18 ms at N = 2^22): a lane outside the mask adds
+    // exactly 0
+    const float w = take ? mr3 : 0.f;
+    bx = fmaf(w, dx, bx);
+    by = fmaf(w, dy, by);
+    bz = fmaf(w, dz, bz);
   }
   acc.add(bx, by, bz);
 }
