@@ -56,6 +56,13 @@ WORKLOADS = {
     "two-spheres-4m": dict(n=1 << 22, theta=0.5, eps=0.001, leaf=8, dt=2e-4, edge=2.0, kind="two", seed=0,
                            desc="two Plummer spheres of 2^21 (B: a=0.1, M=0.1 at (10,0,0)), theta=0.5, "
                                 "eps=0.001, leaf 8, dt=2e-4"),
+    # the reference app's own frame (src/ofApp.h:60,62; src/ofApp.cpp:96; src/HashedOctree.hpp:151):
+    # its solar-system scene in SI units, theta 1, dt 1e-3, softening 0.025, leaf capacity 1, root
+    # edge S, the pseudo-barycentre (literal) multipoles and the unsorted acceleration array
+    "app-solar-4444": dict(n=4444, theta=1.0, eps=0.025, leaf=1, dt=1e-3, edge=1.0, kind="solar", seed=1,
+                           multipole="literal", acc_follows_body=0,
+                           desc="the reference app's frame: SetupSolarSystem scene N=4444 (SI units), theta=1, "
+                                "eps=0.025, leaf 1, dt=1e-3, literal multipoles, root edge S"),
 }
 METRIC = "body-steps/s @theta=0.5, acc err<=1e-3: plain vs batched/adjoint, 1 GB300 vs CPU"
 # algorithmic flops per interaction (an FMA counts 2): point mass 20 (3 sub, r^2 + eps^2 6, rsqrt,
@@ -124,10 +131,34 @@ class Dist:
         return float(t.item())
 
 
-def make_inputs(bh, w, seed):
+def make_inputs(bh, w, seed, sim=None):
+    """Initial (pos_m, vel) float32 (n, 4) arrays of a workload. The solar scene comes from the
+    library's device generator through `sim`, or, without one (the CPU arm), from the oracle's
+    restatement of the same generator (the same draws; within 1e-5 of the device scene)."""
     if w["kind"] == "two":
         return bh.two_spheres(seed, w["n"])
+    if w["kind"] == "solar":
+        n = w["n"]
+        if sim is not None:
+            sim.solar_system_device(seed, n, bh.UNITS_SI)
+            p, v, _ = sim.get_bodies()
+            return np.ascontiguousarray(p), np.ascontiguousarray(v)
+        from oracle.oracle import Restatement
+
+        rows = Restatement().solar_system(seed, n)
+        pm = np.zeros((n, 4), np.float32)
+        vel = np.zeros((n, 4), np.float32)
+        pm[:, :3], pm[:, 3], vel[:, :3] = rows[:, :3], rows[:, 6], rows[:, 3:6]
+        return pm, vel
     return bh.plummer(seed, w["n"])
+
+
+def multipole_mode(bh, w):
+    """(library multipole constant, oracle mode) of a workload: quadrupoles unless it asks for the
+    reference's literal pseudo-barycentres."""
+    if w.get("multipole") == "literal":
+        return bh.BH_MULTIPOLE_LITERAL, 0
+    return bh.BH_MULTIPOLE_QUADRUPOLE, 1
 
 
 class ClockSampler:
@@ -212,7 +243,7 @@ def ncu_traffic():
     return None
 
 
-def accuracy_vs_direct(w, pm, acc_by_theta, orc, nthreads, ntarget=4096, ntarget_walk=65536, tree=None):
+def accuracy_vs_direct(w, pm, acc_by_theta, orc, nthreads, ntarget=4096, ntarget_walk=65536, tree=None, mode=1):
     """Median / p99 relative error of the step-0 accelerations against the FP64 direct sum on a
     seeded subsample (the <= 1e-3 accuracy gate at theta 0.5), for the workload's theta and the others
     of the at-scale sweep; and against the reference's tree walk (the oracle restatement) on a
@@ -237,7 +268,8 @@ def accuracy_vs_direct(w, pm, acc_by_theta, orc, nthreads, ntarget=4096, ntarget
         c, edge = tree
         tw = np.sort(np.random.default_rng(4321).choice(len(pm), min(ntarget_walk, len(pm)),
                                                         replace=False)).astype(np.uint32)
-        ref, _, _ = orc.force(pos, mass, c, edge, w["leaf"], 1, w["theta"], w["eps"], targets=tw, nthreads=nthreads)
+        ref, _, _ = orc.force(pos, mass, c, edge, w["leaf"], mode, w["theta"], w["eps"], targets=tw,
+                              nthreads=nthreads)
         err = relerr(acc_by_theta[w["theta"]][tw], ref)
         res["vs_reference_walk"] = {"median": float(np.median(err)), "p99": float(np.percentile(err, 99)),
                                     "targets": int(len(tw))}
@@ -261,14 +293,14 @@ def cpu_sample(bh, w, pm, nthreads, walk_sample):
     t1 = time.perf_counter()
     rng = np.random.default_rng(99)
     tgt = np.sort(rng.choice(n, min(walk_sample, n), replace=False)).astype(np.uint32)
-    build_s, walk_s, _ = orc.time_sample(sp, sm, c, size * w["edge"], w["leaf"], 1, w["theta"], w["eps"], tgt,
-                                         nthreads=nthreads)
+    build_s, walk_s, _ = orc.time_sample(sp, sm, c, size * w["edge"], w["leaf"], multipole_mode(bh, w)[1],
+                                         w["theta"], w["eps"], tgt, nthreads=nthreads)
     fixed = (t1 - t0) + build_s
     per_step = fixed + walk_s * n / len(tgt)
     return {"value": n / per_step, "unit": "body-steps/s", "cores": nthreads, "kind": "port",
-            "sample": (f"bounds+keys+sort on all {n} bodies ({t1 - t0:.2f} s) + tree build on all {n} "
-                       f"({build_s:.2f} s) + walk of {len(tgt)} sampled bodies ({walk_s:.2f} s) scaled to {n}; "
-                       f"{nthreads} thread(s); extrapolated step {per_step:.1f} s"),
+            "sample": (f"bounds+keys+sort on all {n} bodies ({t1 - t0:.3g} s) + tree build on all {n} "
+                       f"({build_s:.3g} s) + walk of {len(tgt)} sampled bodies ({walk_s:.3g} s) scaled to {n}; "
+                       f"{nthreads} thread(s); extrapolated step {per_step:.3g} s"),
             "seconds_per_step": per_step}
 
 
@@ -325,10 +357,11 @@ def run_ours(args, w, dist):
     bh = __graft_entry__.package()
     bh.load()
     n = w["n"]
-    pm, vel = make_inputs(bh, w, w["seed"] + dist.rank)
+    mp, mode = multipole_mode(bh, w)
     prm = bh.default_params(theta=w["theta"], eps=w["eps"], dt=w["dt"], leaf_capacity=w["leaf"],
-                            multipole=bh.BH_MULTIPOLE_QUADRUPOLE, edge_factor=w["edge"], acc_follows_body=1)
+                            multipole=mp, edge_factor=w["edge"], acc_follows_body=w.get("acc_follows_body", 1))
     sim = dist.simulation(bh, n)
+    pm, vel = make_inputs(bh, w, w["seed"] + dist.rank, sim)
     sim.set_bodies(pm, vel)
 
     # step-0 accelerations for the accuracy gate (rank 0, before stepping)
@@ -337,10 +370,10 @@ def run_ours(args, w, dist):
         from oracle.oracle import Restatement
 
         c, size = sim.bounds()
-        sim.build(c, size * w["edge"], w["leaf"], bh.BH_MULTIPOLE_QUADRUPOLE)
+        sim.build(c, size * w["edge"], w["leaf"], mp)
         accs = {th: sim.force(th, w["eps"]) for th in sorted({0.3, 0.5, 0.7, w["theta"]})}
         accuracy = accuracy_vs_direct(w, pm, accs, Restatement(), os.cpu_count() or 1,
-                                      tree=(c, size * w["edge"]))
+                                      tree=(c, size * w["edge"]), mode=mode)
         sim.set_bodies(pm, vel)
 
     fp32_peak = sim.fp32_peak_tflops()
@@ -353,6 +386,8 @@ def run_ours(args, w, dist):
     energy0 = sim.energy(w["theta"], w["eps"])  # over the tree of the last warm-up step
 
     gpu_index = dist.gpu_index()
+    # a literal cell is a point mass at its pseudo-barycentre (Q = 0): the point-mass flops
+    cell_flops = FLOPS_CELL_QUAD if mode == 1 else FLOPS_P2P
     per_step_ms, walk_ms, sort_ms, flops, inter, util_cell, util_pt = [], [], [], [], [], [], []
     stage = {}
     launches = 0
@@ -366,7 +401,7 @@ def run_ours(args, w, dist):
             per_step_ms.append(st.ms_step)
             walk_ms.append(st.ms_walk)
             sort_ms.append(st.ms_sort)
-            flops.append(FLOPS_P2P * st.interactions_p2p + FLOPS_CELL_QUAD * st.interactions_cell)
+            flops.append(FLOPS_P2P * st.interactions_p2p + cell_flops * st.interactions_cell)
             inter.append(st.interactions_p2p + st.interactions_cell)
             util_cell.append((st.interactions_cell, st.walk_cell_evals))
             util_pt.append((st.interactions_p2p, st.walk_point_evals))
@@ -441,7 +476,7 @@ def run_ours(args, w, dist):
                 "ms_per_step": statistics.median(e2e_ms)},
         "interactions_per_s": dist.sum(sum(inter)) / (total_ms * 1e-3),
         "interactions_per_body": statistics.mean(inter) / n,
-        "roofline": {"kernel": "k_walk<quadrupole>", "bound": "fp32", "achieved": achieved_tflops,
+        "roofline": {"kernel": "k_walk<quadrupole>" if mode == 1 else "k_walk<literal>", "bound": "fp32", "achieved": achieved_tflops,
                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved_tflops / fp32_peak,
                      "peak_source": "measured FP32 FMA peak of this GPU (bh_measure_fp32_peak)",
                      "traffic": walk_traffic,
@@ -523,7 +558,7 @@ def run_ensemble(args, dist):
             launches += st.kernel_launches
             per_step.append(st.ms_step)
             walk_ms.append(st.ms_walk)
-            flops.append(FLOPS_P2P * st.interactions_p2p + FLOPS_CELL_QUAD * st.interactions_cell)
+            flops.append(FLOPS_P2P * st.interactions_p2p + cell_flops * st.interactions_cell)
             for key, val in st.as_dict().items():
                 if key.startswith("ms_"):
                     stage[key] = stage.get(key, 0.0) + val

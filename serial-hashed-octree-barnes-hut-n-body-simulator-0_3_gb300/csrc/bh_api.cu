@@ -231,6 +231,7 @@ bh_status bh_create(bh_ctx** out, size_t capacity, int device) {
   if (cudaSetDevice(device) != cudaSuccess) return BH_ERR_DEVICE;
   bh::sort_init();
   bh::walk_init();
+  bh::tree_init();
   bh_ctx* c = new (std::nothrow) bh_ctx();
   if (!c) return BH_ERR_OOM;
   c->device = device;

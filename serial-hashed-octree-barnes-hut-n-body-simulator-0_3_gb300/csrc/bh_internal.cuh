@@ -23,6 +23,10 @@ constexpr int kNumEvents = 64;
 // Levels with at most this many nodes are built one warp per node (tiles of 8 nodes): one
 // resident wave of the build's 608 blocks x 8 warps.
 constexpr int kLevelWarpNodes = 4864;
+// Systems of at most this many bodies are sorted and built by one block each (the keys fit in
+// one SM's shared memory), so those stages are one launch each instead of one per digit or
+// per level.
+constexpr int kSmallMax = 16384;
 
 // Device error word bits. bit = (bh_status code - 3), so the host maps them back.
 enum : uint32_t {
@@ -246,6 +250,7 @@ void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t*
 int sort_max_tiles(size_t n);
 void sort_init();
 void walk_init();
+void tree_init();
 
 void launch_bounds(bh_ctx* c, const float4* pos, int n, double edge_factor);
 void launch_set_geom(bh_ctx* c, const double center[3], double size, const double tcenter[3], double tedge);

@@ -253,6 +253,79 @@ __global__ __launch_bounds__(kThreads, BH_SORT_MIN_BLOCKS) void k_onesweep(const
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Small sorts by rank counting. Each key's output position is the number of keys that sort
+// before it: the smaller keys, and the equal keys earlier in the input (which makes the sort
+// stable). A block takes 32 consecutive keys i, one per lane, and its eight warps split each
+// staged tile of keys j into eighths; all lanes of a warp compare their key with the same j (a
+// shared-memory broadcast), and the block adds the eight partial counts. That is n^2
+// comparisons spread over the whole GPU (about 20 M at 4 444 keys), where the eight digit passes
+// of a radix sort are a chain of launches, or of barriers inside one block, that costs far more
+// at this size.
+// ---------------------------------------------------------------------------------------
+constexpr int kRankThreads = 256;
+constexpr int kRankParts = kRankThreads / 32;
+constexpr int kRankTile = 2048;  // keys j staged per round (16 KB)
+
+__global__ __launch_bounds__(kThreads) void k_copy_pairs(const uint64_t* __restrict__ kin,
+                                                         const uint32_t* __restrict__ vin,
+                                                         uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                         int n) {
+  const int i = blockIdx.x * kThreads + threadIdx.x;
+  if (i < n) {
+    kout[i] = kin[i];
+    vout[i] = vin[i];
+  }
+}
+
+__global__ __launch_bounds__(kRankThreads) void k_sort_rank(const uint64_t* __restrict__ kin,
+                                                            const uint32_t* __restrict__ vin,
+                                                            uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                            int n) {
+  __shared__ uint64_t s_k[kRankTile];
+  __shared__ uint32_t s_cnt[kRankParts][32];
+  const int lane = threadIdx.x & 31, part = threadIdx.x >> 5;
+  const int base = blockIdx.x * 32, i = base + lane;
+  const bool valid = i < n;
+  const uint64_t ki = valid ? kin[i] : 0ull;
+  uint32_t cnt = 0;
+  // the keys j come through shared memory a tile at a time (one coalesced read of the tile by the
+  // block, instead of a chain of dependent-latency broadcast reads from L2 per warp); warp `part`
+  // compares its lanes' keys with its eighth of the tile
+  for (int t0 = 0; t0 < n; t0 += kRankTile) {
+    const int m = min(kRankTile, n - t0);
+#pragma unroll
+    for (int r = 0; r < kRankTile / kRankThreads; ++r) {
+      const int q = r * kRankThreads + threadIdx.x;
+      if (q < m) s_k[q] = kin[t0 + q];
+    }
+    __syncthreads();
+    const int j0 = t0 + part * (kRankTile / kRankParts);
+    const int j1 = min(t0 + m, j0 + kRankTile / kRankParts);
+    const uint64_t* sk = s_k - t0;  // sk[j] is key j
+    const int below = min(j1, base);  // j before all of this warp's keys: equal keys sort first
+#pragma unroll 8
+    for (int j = j0; j < below; ++j) cnt += sk[j] <= ki ? 1u : 0u;
+    const int d1 = min(j1, base + 32);  // this warp's own keys: equal ones sort first when j < i
+    for (int j = max(j0, base); j < d1; ++j) {
+      const uint64_t kj = sk[j];
+      cnt += (kj < ki || (kj == ki && j < i)) ? 1u : 0u;
+    }
+#pragma unroll 8
+    for (int j = max(j0, base + 32); j < j1; ++j) cnt += sk[j] < ki ? 1u : 0u;  // after: equal keys sort later
+    __syncthreads();
+  }
+  s_cnt[part][lane] = cnt;
+  __syncthreads();
+  if (part == 0 && valid) {
+    uint32_t r = 0;
+#pragma unroll
+    for (int q = 0; q < kRankParts; ++q) r += s_cnt[q][lane];
+    kout[r] = ki;
+    vout[r] = vin[i];
+  }
+}
+
 }  // namespace
 
 int sort_max_tiles(size_t n) { return (int)((n + kTile - 1) / kTile); }
@@ -272,8 +345,15 @@ void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t*
   if (n <= 1) return;
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_onesweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(OnesweepSmem));
+    sort_init();
     attr_set = true;
+  }
+  if (n <= kSmallMax && first_pass == 0 && npasses == kPasses) {
+    // the result goes back to keys_in / vals_in, as after the eight digit passes
+    c->launches += 2;
+    k_copy_pairs<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(keys_in, vals_in, keys_tmp, vals_tmp, n);
+    k_sort_rank<<<(n + 31) / 32, kRankThreads, 0, st>>>(keys_tmp, vals_tmp, keys_in, vals_in, n);
+    return;
   }
   const int tiles = sort_max_tiles((size_t)n);
   cudaMemsetAsync(c->sort.hist, 0, sizeof(uint32_t) * kPasses * kRadix, st);

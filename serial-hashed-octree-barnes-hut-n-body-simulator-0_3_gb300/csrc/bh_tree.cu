@@ -693,6 +693,134 @@ __global__ __launch_bounds__(kThreads) void k_level(int d, const uint64_t* __res
   }
 }
 
+// The whole build of a system of at most kSmallMax bodies in one block: the sorted tree keys
+// are staged in shared memory, the block runs the levels one after another with barriers in
+// between, and a running child offset takes the place of the look-back. It writes the same
+// records in the same order as k_tree_init followed by the k_level launches (the nodes of a
+// level in key order, their children appended after the level in the same order).
+//
+// Nothing the block needs is read back from global memory: a node's key is its first body's
+// tree key cut to the node's depth (the key's marker bit is bit 63), and the body ranges of the
+// next level stay in a shared-memory buffer when the level has at most `cap` nodes (a level has
+// at most n nodes, so below about 8 000 bodies every level does).
+constexpr int kBuildSmallThreads = 1024;
+constexpr int kBuildSmallWarps = kBuildSmallThreads / 32;
+constexpr size_t kBuildSmallSmem = 200 * 1024;  // keys + two levels of ranges
+
+__host__ __device__ inline int build_small_cap(int n) {
+  const long long c = ((long long)kBuildSmallSmem - 8ll * n) / (2 * (long long)sizeof(int2));
+  return (int)(c < n ? c : n);
+}
+
+__global__ __launch_bounds__(kBuildSmallThreads, 1) void k_build_small(
+    int n, const uint64_t* __restrict__ tkey, int leaf_cap, uint64_t* __restrict__ nkey, int2* __restrict__ nrange,
+    WalkNode* __restrict__ wn, uint8_t* __restrict__ childbyte, int* __restrict__ level_bounds, long long node_cap,
+    uint32_t* __restrict__ err) {
+  extern __shared__ __align__(16) uint64_t s_key[];
+  __shared__ uint32_t s_wex[kBuildSmallWarps];
+  __shared__ uint32_t s_total;
+  __shared__ int s_bounds[kLevels + 2];
+  __shared__ int s_full;  // a level ran out of node capacity: later levels add nothing
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int cap = build_small_cap(n);
+  int2* s_rng[2] = {reinterpret_cast<int2*>(s_key + n), reinterpret_cast<int2*>(s_key + n) + cap};
+  for (int i = t; i < n; i += kBuildSmallThreads) s_key[i] = tkey[i];
+  if (t <= kLevels + 1) s_bounds[t] = (t == 0) ? 0 : (t == 1 ? (n > 0 ? 1 : 0) : -1);
+  if (t == 0) {
+    s_full = 0;
+    if (n > 0) {
+      nkey[0] = 1ull;
+      nrange[0] = make_int2(0, n);
+      s_rng[0][0] = make_int2(0, n);
+    }
+  }
+  __syncthreads();
+  for (int d = 0; d < kLevels; ++d) {
+    const int lo = s_bounds[d], hi = s_bounds[d + 1];
+    const int shift = 3 * (kMaxDepth - 1 - d);
+    const bool on_chip = hi - lo <= cap;  // this level's ranges are in s_rng[d & 1]
+    const int2* cur = s_rng[d & 1];
+    int2* nxt = s_rng[(d + 1) & 1];
+    int next = hi;  // index of the next child of this level
+    if (hi > lo && !s_full) {
+      for (int base = lo; base < hi; base += kBuildSmallThreads) {
+        const int node = base + t;
+        const bool valid = node < hi;
+        int2 r = make_int2(0, 0);
+        int bnd[9];
+        int nc = 0;
+        uint32_t mask = 0;
+        bool internal = false;
+        if (valid) {
+          r = on_chip ? cur[node - lo] : nrange[node];
+          internal = r.y > leaf_cap && d < kMaxDepth;
+          if (internal) {
+            bnd[0] = r.x;
+            bnd[8] = r.x + r.y;
+            split_search<1, 4>(s_key, shift, bnd);
+            split_search<2, 2>(s_key, shift, bnd);
+            split_search<4, 1>(s_key, shift, bnd);
+            for (int v = 0; v < 8; ++v)
+              if (bnd[v + 1] > bnd[v]) {
+                ++nc;
+                mask |= 1u << v;
+              }
+          }
+        }
+        // block exclusive scan of the child counts
+        uint32_t x = (uint32_t)nc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x += y;
+        }
+        if (lane == 31) s_wex[w] = x;
+        __syncthreads();
+        if (w == 0) {
+          const uint32_t v = s_wex[lane];
+          uint32_t z = v;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
+            if (lane >= o) z += y;
+          }
+          s_wex[lane] = z - v;
+          if (lane == 31) s_total = z;
+        }
+        __syncthreads();
+        const long long child_base = (long long)next + (x - (uint32_t)nc + s_wex[w]);
+        if (valid) {
+          const bool fits = child_base + nc <= node_cap;
+          if (!fits) {
+            atomicOr(err, kErrNodes);
+            s_full = 1;
+          }
+          const bool make = internal && fits;
+          if (make) {
+            const uint64_t pk = s_key[r.x] >> (3 * (kMaxDepth - d));  // this node's key
+            int k = 0;
+            for (int v = 0; v < 8; ++v) {
+              if (!(mask & (1u << v))) continue;
+              const int ci = (int)child_base + k++;
+              const int2 cr = make_int2(bnd[v], bnd[v + 1] - bnd[v]);
+              nkey[ci] = (pk << 3) | (uint64_t)v;
+              nrange[ci] = cr;
+              if (ci - hi < cap) nxt[ci - hi] = cr;
+            }
+          }
+          wn[node].link = make_int4(make ? (int)child_base : -1, make ? nc : 0, r.x, r.y);
+          childbyte[node] = (uint8_t)(make ? mask : 0u);
+        }
+        next += (int)s_total;
+        __syncthreads();  // s_wex and s_total are reused; this tile's children are complete
+      }
+    }
+    if (t == 0) s_bounds[d + 2] = next;
+    __syncthreads();
+  }
+  if (t <= kLevels + 1) level_bounds[t] = s_bounds[t];
+}
+
 // ---------------------------------------------------------------------------------------
 // upsweep
 // ---------------------------------------------------------------------------------------
@@ -1161,7 +1289,20 @@ void launch_gather_tree(bh_ctx* c, const uint32_t* tslot, int n, const float4* p
   if (n > 0) k_gather_tree<<<grid_for(n), kThreads, 0, c->stream>>>(tslot, n, pos, tpos);
 }
 
+// Function attributes set once per process, before any stream capture.
+void tree_init() {
+  cudaFuncSetAttribute(k_build_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBuildSmallSmem);
+}
+
 void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
+  if (!batch && n <= kSmallMax) {
+    c->launches += 1;
+    const size_t smem = 8 * (size_t)n + 2 * sizeof(int2) * (size_t)build_small_cap(n);  // <= kBuildSmallSmem
+    k_build_small<<<1, kBuildSmallThreads, smem, c->stream>>>(
+        n, c->tkey, leaf_cap, c->nkey, c->nrange, c->wnode, c->nchildbyte, c->level_bounds, (long long)c->node_cap,
+        c->err);
+    return;
+  }
   c->launches += 1 + kLevels;
   if (batch)
     k_tree_init_batch<<<(max(c->nsys, kLevels + 2) + 255) / 256, 256, 0, c->stream>>>(

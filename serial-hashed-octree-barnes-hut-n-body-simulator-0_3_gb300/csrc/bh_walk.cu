@@ -666,10 +666,15 @@ void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc
     else
       launch_quad_variant(c, c->walk_variant, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
   } else {
+    // the literal walk has no tuned variants: its group size follows N, the largest of 32, 16
+    // and 8 bodies that still gives at least 1024 groups (about seven warps per SM; the tuned
+    // quadrupole walk picks 8 at 4 444 bodies, 16 at 16 384 and 32 at 2^22)
+    int gsize = 32;
+    while (gsize > 8 && (n + gsize - 1) / gsize < 1024) gsize /= 2;
     if (self)
-      launch_walk_t<false, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
+      launch_walk_t<false, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, gsize);
     else
-      launch_walk_t<false, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
+      launch_walk_t<false, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, gsize);
   }
 }
 
