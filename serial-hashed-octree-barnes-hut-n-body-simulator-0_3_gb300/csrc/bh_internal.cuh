@@ -23,10 +23,6 @@ constexpr int kNumEvents = 64;
 // Levels with at most this many nodes are built one warp per node (tiles of 8 nodes): one
 // resident wave of the build's 608 blocks x 8 warps.
 constexpr int kLevelWarpNodes = 4864;
-// Systems of at most this many bodies are sorted and built by one block each (the keys fit in
-// one SM's shared memory), so those stages are one launch each instead of one per digit or
-// per level.
-constexpr int kSmallMax = 16384;
 
 // Device error word bits. bit = (bh_status code - 3), so the host maps them back.
 enum : uint32_t {

@@ -266,6 +266,9 @@ __global__ __launch_bounds__(kThreads, BH_SORT_MIN_BLOCKS) void k_onesweep(const
 constexpr int kRankThreads = 256;
 constexpr int kRankParts = kRankThreads / 32;
 constexpr int kRankTile = 2048;  // keys j staged per round (16 KB)
+// Sorts of at most this many keys go by rank: at 4 444 keys 16 us against the radix sort's
+// 68 us, at 16 384 keys 66 us against 74 us (the n^2 comparisons catch up beyond).
+constexpr int kRankSortMax = 16384;
 
 __global__ __launch_bounds__(kThreads) void k_copy_pairs(const uint64_t* __restrict__ kin,
                                                          const uint32_t* __restrict__ vin,
@@ -348,7 +351,7 @@ void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t*
     sort_init();
     attr_set = true;
   }
-  if (n <= kSmallMax && first_pass == 0 && npasses == kPasses) {
+  if (n <= kRankSortMax && first_pass == 0 && npasses == kPasses) {
     // the result goes back to keys_in / vals_in, as after the eight digit passes
     c->launches += 2;
     k_copy_pairs<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(keys_in, vals_in, keys_tmp, vals_tmp, n);

@@ -693,37 +693,34 @@ __global__ __launch_bounds__(kThreads) void k_level(int d, const uint64_t* __res
   }
 }
 
-// The whole build of a system of at most kSmallMax bodies in one block: the sorted tree keys
-// are staged in shared memory, the block runs the levels one after another with barriers in
-// between, and a running child offset takes the place of the look-back. It writes the same
+// The whole build of a system of at most kBuildSmallMax bodies in one block: the sorted tree
+// keys are staged in shared memory, the block runs the levels one after another with barriers
+// in between, and a running child offset takes the place of the look-back. It writes the same
 // records in the same order as k_tree_init followed by the k_level launches (the nodes of a
 // level in key order, their children appended after the level in the same order).
 //
 // Nothing the block needs is read back from global memory: a node's key is its first body's
 // tree key cut to the node's depth (the key's marker bit is bit 63), and the body ranges of the
-// next level stay in a shared-memory buffer when the level has at most `cap` nodes (a level has
-// at most n nodes, so below about 8 000 bodies every level does).
+// next level go to a shared-memory buffer as well as to nrange (a level has at most n nodes).
+// The block's cost grows with the levels' node counts, the multi-block build's with the
+// number of levels: at the app's 4 444-body scene (22 levels) one block took 129 us against
+// 160 us, at a 16 384-body Plummer sphere 168 us against 139 us.
+constexpr int kBuildSmallMax = 8192;
 constexpr int kBuildSmallThreads = 1024;
 constexpr int kBuildSmallWarps = kBuildSmallThreads / 32;
-constexpr size_t kBuildSmallSmem = 200 * 1024;  // keys + two levels of ranges
-
-__host__ __device__ inline int build_small_cap(int n) {
-  const long long c = ((long long)kBuildSmallSmem - 8ll * n) / (2 * (long long)sizeof(int2));
-  return (int)(c < n ? c : n);
-}
+constexpr size_t kBuildSmallSmem = (sizeof(uint64_t) + 2 * sizeof(int2)) * kBuildSmallMax;  // 192 KB
 
 __global__ __launch_bounds__(kBuildSmallThreads, 1) void k_build_small(
     int n, const uint64_t* __restrict__ tkey, int leaf_cap, uint64_t* __restrict__ nkey, int2* __restrict__ nrange,
     WalkNode* __restrict__ wn, uint8_t* __restrict__ childbyte, int* __restrict__ level_bounds, long long node_cap,
     uint32_t* __restrict__ err) {
-  extern __shared__ __align__(16) uint64_t s_key[];
+  extern __shared__ __align__(16) uint64_t s_key[];  // n keys, then two levels of n ranges
   __shared__ uint32_t s_wex[kBuildSmallWarps];
   __shared__ uint32_t s_total;
   __shared__ int s_bounds[kLevels + 2];
   __shared__ int s_full;  // a level ran out of node capacity: later levels add nothing
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  const int cap = build_small_cap(n);
-  int2* s_rng[2] = {reinterpret_cast<int2*>(s_key + n), reinterpret_cast<int2*>(s_key + n) + cap};
+  int2* const s_rng = reinterpret_cast<int2*>(s_key + n);
   for (int i = t; i < n; i += kBuildSmallThreads) s_key[i] = tkey[i];
   if (t <= kLevels + 1) s_bounds[t] = (t == 0) ? 0 : (t == 1 ? (n > 0 ? 1 : 0) : -1);
   if (t == 0) {
@@ -731,17 +728,16 @@ __global__ __launch_bounds__(kBuildSmallThreads, 1) void k_build_small(
     if (n > 0) {
       nkey[0] = 1ull;
       nrange[0] = make_int2(0, n);
-      s_rng[0][0] = make_int2(0, n);
+      s_rng[0] = make_int2(0, n);
     }
   }
   __syncthreads();
   for (int d = 0; d < kLevels; ++d) {
     const int lo = s_bounds[d], hi = s_bounds[d + 1];
     const int shift = 3 * (kMaxDepth - 1 - d);
-    const bool on_chip = hi - lo <= cap;  // this level's ranges are in s_rng[d & 1]
-    const int2* cur = s_rng[d & 1];
-    int2* nxt = s_rng[(d + 1) & 1];
-    int next = hi;  // index of the next child of this level
+    const int2* cur = s_rng + (d & 1) * n;  // this level's ranges, by node - lo
+    int2* nxt = s_rng + ((d + 1) & 1) * n;  // the next level's, by node - hi
+    int next = hi;                          // index of the next child of this level
     if (hi > lo && !s_full) {
       for (int base = lo; base < hi; base += kBuildSmallThreads) {
         const int node = base + t;
@@ -752,7 +748,7 @@ __global__ __launch_bounds__(kBuildSmallThreads, 1) void k_build_small(
         uint32_t mask = 0;
         bool internal = false;
         if (valid) {
-          r = on_chip ? cur[node - lo] : nrange[node];
+          r = cur[node - lo];
           internal = r.y > leaf_cap && d < kMaxDepth;
           if (internal) {
             bnd[0] = r.x;
@@ -805,7 +801,7 @@ __global__ __launch_bounds__(kBuildSmallThreads, 1) void k_build_small(
               const int2 cr = make_int2(bnd[v], bnd[v + 1] - bnd[v]);
               nkey[ci] = (pk << 3) | (uint64_t)v;
               nrange[ci] = cr;
-              if (ci - hi < cap) nxt[ci - hi] = cr;
+              nxt[ci - hi] = cr;  // ci - hi < n: a level has at most n nodes
             }
           }
           wn[node].link = make_int4(make ? (int)child_base : -1, make ? nc : 0, r.x, r.y);
@@ -1295,9 +1291,9 @@ void tree_init() {
 }
 
 void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
-  if (!batch && n <= kSmallMax) {
+  if (!batch && n <= kBuildSmallMax) {
     c->launches += 1;
-    const size_t smem = 8 * (size_t)n + 2 * sizeof(int2) * (size_t)build_small_cap(n);  // <= kBuildSmallSmem
+    const size_t smem = (sizeof(uint64_t) + 2 * sizeof(int2)) * (size_t)n;  // <= kBuildSmallSmem
     k_build_small<<<1, kBuildSmallThreads, smem, c->stream>>>(
         n, c->tkey, leaf_cap, c->nkey, c->nrange, c->wnode, c->nchildbyte, c->level_bounds, (long long)c->node_cap,
         c->err);

@@ -167,9 +167,9 @@ def test_coincident_bodies_bucket_at_depth21(bh, orc, sim):
     assert np.all(np.isfinite(acc))
 
 
-# up to 16 384 bodies the sorts and the build run in one block each; 16 385 takes the
-# multi-block kernels
-@pytest.mark.parametrize("n", [1, 2, 3, 31, 32, 33, 1000, 1025, 4097, 16383, 16384, 16385])
+# the sorts go by rank up to 16 384 keys and the build runs in one block up to 8 192 bodies;
+# the sizes either side of both limits take both paths
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 32, 33, 1000, 1025, 4097, 8192, 8193, 16384, 16385])
 def test_small_and_ragged_n(bh, orc, sim, n):
     pm, v = bh.plummer(300 + n, n)
     sim.set_bodies(pm, v)
