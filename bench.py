@@ -488,14 +488,14 @@ def run_ours(args, w, dist):
                           "bytes_per_launch": sort_bytes},
         # node discovery + multipoles: N x 24 B (keys, positions) + M x (64 + 16) B (walk records,
         # node keys and ranges) + M x 64 B (upsweep records), M = nodes of the step
-        "roofline_build": {"kernel": "k_level x 22 + k_upsweep_links + k_upsweep", "bound": "hbm",
+        "roofline_build": {"kernel": "k_nodes_count/scan/write/link + k_upsweep_links + k_upsweep", "bound": "hbm",
                            "achieved": build_bytes / (build_ms * 1e-3) / 1e9 if build_ms > 0 else None,
                            "peak": hbm_peak, "unit": "GB/s",
                            "frac": (build_bytes / (build_ms * 1e-3) / 1e9 / hbm_peak) if hbm_peak and build_ms > 0
                            else None,
                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
                            "bytes_per_step": build_bytes, "nodes": nodes,
-                           "note": "latency-bound: dependent binary searches per level, float-float chains per leaf (see profiles)"},
+                           "note": "node records at all depths at once; the upsweep is latency-bound (float-float chains per leaf, see profiles)"},
         "stage_ms_per_step": {k[3:]: v / args.steps for k, v in stage.items()},
         "walk_lane_utilization": {
             "cells": sum(a for a, _ in util_cell) / max(1, 32 * sum(b for _, b in util_cell)),

@@ -693,128 +693,245 @@ __global__ __launch_bounds__(kThreads) void k_level(int d, const uint64_t* __res
   }
 }
 
-// The whole build of a system of at most kBuildSmallMax bodies in one block: the sorted tree
-// keys are staged in shared memory, the block runs the levels one after another with barriers
-// in between, and a running child offset takes the place of the look-back. It writes the same
-// records in the same order as k_tree_init followed by the k_level launches (the nodes of a
-// level in key order, their children appended after the level in the same order).
-//
-// Nothing the block needs is read back from global memory: a node's key is its first body's
-// tree key cut to the node's depth (the key's marker bit is bit 63), and the body ranges of the
-// next level go to a shared-memory buffer as well as to nrange (a level has at most n nodes).
-// The block's cost grows with the levels' node counts, the multi-block build's with the
-// number of levels: at the app's 4 444-body scene (22 levels) one block took 129 us against
-// 160 us, at a 16 384-body Plummer sphere 168 us against 139 us.
-constexpr int kBuildSmallMax = 8192;
-constexpr int kBuildSmallThreads = 1024;
-constexpr int kBuildSmallWarps = kBuildSmallThreads / 32;
-constexpr size_t kBuildSmallSmem = (sizeof(uint64_t) + 2 * sizeof(int2)) * kBuildSmallMax;  // 192 KB
+// ---------------------------------------------------------------------------------------
+// Parallel build: every depth at once
+// ---------------------------------------------------------------------------------------
+// The same node set, order and records as k_tree_init + k_level, without a chain of levels.
+// With the tree keys sorted, a depth-e cell is a contiguous run of bodies, and:
+//   * the depth-e cell of body i holds more than L bodies exactly when some run of L + 1
+//     consecutive bodies containing i shares its first e digits; the keys being sorted, a run
+//     [j, j + L] shares as many digits as its end keys do. So with w(j) = digits shared by keys j
+//     and j + L, E(i) = max of w(j) over j in [i - L, i] is the deepest such depth;
+//   * a node of depth d >= 1 is a non-empty cell whose parent cell holds more than L bodies
+//     (the parent's parent then does too), so a depth-d node starts at body i exactly when keys
+//     i - 1 and i differ in the first d digits and d <= E(i) + 1 (and d <= 21): every depth
+//     from (digits shared with key i - 1) + 1 to min(E(i) + 1, 21).
+// The build counts node starts per depth for each tile of bodies (k_nodes_count), scans the
+// counts of each depth over the tiles (k_nodes_scan), writes every node from the thread of its
+// first body (k_nodes_write: index = level start + starts of its depth before it; its cell's
+// end by a galloping search; its first child is node (d + 1, i); its parent is the last
+// depth-(d - 1) node starting at or before i), and lets each parent's last child set the
+// parent's child count and child byte (k_nodes_link).
+constexpr int kPBThreads = 512;
+constexpr int kPBWarps = kPBThreads / 32;
+constexpr int kPBMaxLeaf = 64;  // halo of the window maxima; larger leaf capacities use k_level
 
-__global__ __launch_bounds__(kBuildSmallThreads, 1) void k_build_small(
-    int n, const uint64_t* __restrict__ tkey, int leaf_cap, uint64_t* __restrict__ nkey, int2* __restrict__ nrange,
-    WalkNode* __restrict__ wn, uint8_t* __restrict__ childbyte, int* __restrict__ level_bounds, long long node_cap,
-    uint32_t* __restrict__ err) {
-  extern __shared__ __align__(16) uint64_t s_key[];  // n keys, then two levels of n ranges
-  __shared__ uint32_t s_wex[kBuildSmallWarps];
-  __shared__ uint32_t s_total;
-  __shared__ int s_bounds[kLevels + 2];
-  __shared__ int s_full;  // a level ran out of node capacity: later levels add nothing
+// Octal digits (from the top) that two tree keys share; 21 when they are equal (the marker bit
+// 63 is set in both).
+__device__ __forceinline__ int common_digits(uint64_t a, uint64_t b) {
+  const uint64_t x = a ^ b;
+  return x ? (__clzll((long long)x) - 1) / 3 : kMaxDepth;
+}
+
+// Per-warp counts of node starts for each depth 1..21 (ballots only over the depths the warp's
+// bodies start nodes at; a warp of 32 neighbouring bodies spans a few depths of the 21).
+__device__ __forceinline__ void warp_start_counts(int lo, int hi, uint32_t (*s_wc)[kPBWarps]) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int wlo = __reduce_min_sync(0xffffffffu, lo), whi = __reduce_max_sync(0xffffffffu, hi);
+  for (int d = 1 + lane; d <= kMaxDepth; d += 32)
+    if (d < wlo || d > whi) s_wc[d - 1][w] = 0u;
+  for (int d = wlo; d <= whi; ++d) {
+    const unsigned b = __ballot_sync(0xffffffffu, lo <= d && d <= hi);
+    if (lane == 0) s_wc[d - 1][w] = (uint32_t)__popc(b);
+  }
+}
+
+// Start depths of the tile's bodies: lo | hi << 8 (none when lo > hi), and per-warp counts of
+// starts for each depth 1..21 in s_wc.
+__device__ void node_start_depths(const uint64_t* __restrict__ tkey, int n, int leaf_cap, int t0,
+                                  uint32_t (*s_wc)[kPBWarps], uint32_t* span_out) {
+  __shared__ uint64_t s_k[kPBThreads + 2 * kPBMaxLeaf];
+  __shared__ int8_t s_w[kPBThreads + kPBMaxLeaf];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5, L = leaf_cap;
+  const int base = t0 - L;  // s_k[x - base] is key x, for x in [t0 - L, t0 + T + L)
+  for (int x = t; x < kPBThreads + 2 * L; x += kPBThreads) {
+    const int g = base + x;
+    s_k[x] = (g >= 0 && g < n) ? tkey[g] : 0ull;
+  }
+  __syncthreads();
+  for (int x = t; x < kPBThreads + L; x += kPBThreads) {  // w(j) for j in [t0 - L, t0 + T)
+    const int j = base + x;
+    s_w[x] = (int8_t)((j >= 0 && j + L < n) ? common_digits(s_k[x], s_k[x + L]) : -1);
+  }
+  __syncthreads();
+  const int i = t0 + t;
+  int lo = 1, hi = 0;
+  if (i < n) {
+    const uint64_t ki = s_k[i - base];
+    const int lcp = i == 0 ? -1 : common_digits(s_k[i - 1 - base], ki);
+    int e = -1;
+    for (int q = 0; q <= L; ++q) e = max(e, (int)s_w[t + q]);  // j = i - L + q
+    lo = max(lcp + 1, 1);
+    hi = min(e + 1, kMaxDepth);
+  }
+  if (i < n) span_out[i] = (uint32_t)lo | ((uint32_t)hi << 8);
+  warp_start_counts(lo, hi, s_wc);
+  __syncthreads();
+}
+
+__global__ __launch_bounds__(kPBThreads) void k_nodes_count(const uint64_t* __restrict__ tkey, int n, int leaf_cap,
+                                                            uint32_t* __restrict__ span,
+                                                            uint32_t* __restrict__ tile_cnt, int ntiles) {
+  __shared__ uint32_t s_wc[kMaxDepth][kPBWarps];
+  node_start_depths(tkey, n, leaf_cap, blockIdx.x * kPBThreads, s_wc, span);
+  if (threadIdx.x < kMaxDepth) {
+    uint32_t c = 0;
+    for (int q = 0; q < kPBWarps; ++q) c += s_wc[threadIdx.x][q];
+    tile_cnt[(size_t)threadIdx.x * ntiles + blockIdx.x] = c;
+  }
+}
+
+// Block d - 1 scans depth d's tile counts (exclusive, in place) and stores the depth's total.
+__global__ __launch_bounds__(1024) void k_nodes_scan(uint32_t* __restrict__ tile_cnt, int ntiles,
+                                                     uint32_t* __restrict__ totals) {
+  __shared__ uint32_t s_warp[32];
+  uint32_t* c = tile_cnt + (size_t)blockIdx.x * ntiles;
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  int2* const s_rng = reinterpret_cast<int2*>(s_key + n);
-  for (int i = t; i < n; i += kBuildSmallThreads) s_key[i] = tkey[i];
-  if (t <= kLevels + 1) s_bounds[t] = (t == 0) ? 0 : (t == 1 ? (n > 0 ? 1 : 0) : -1);
+  const int per = (ntiles + 1023) / 1024, a = min(ntiles, t * per), b = min(ntiles, a + per);
+  uint32_t sum = 0;
+  for (int q = a; q < b; ++q) sum += c[q];
+  uint32_t x = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    const uint32_t v = s_warp[lane];
+    uint32_t z = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
+      if (lane >= o) z += y;
+    }
+    s_warp[lane] = z - v;
+    if (lane == 31) totals[blockIdx.x] = z;
+  }
+  __syncthreads();
+  uint32_t run = x - sum + s_warp[w];
+  for (int q = a; q < b; ++q) {
+    const uint32_t v = c[q];
+    c[q] = run;
+    run += v;
+  }
+}
+
+// Level starts (s_lb, from the depth totals) and, per depth and warp of this tile, the index of
+// the warp's first node start (s_first); returns the node count.
+__device__ long long node_first_indices(int n, uint32_t lo, uint32_t hi, const uint32_t* __restrict__ tile_excl,
+                                        int ntiles, const uint32_t* __restrict__ totals, long long* s_lb,
+                                        uint32_t (*s_first)[kPBWarps]) {
+  const int t = threadIdx.x;
   if (t == 0) {
-    s_full = 0;
-    if (n > 0) {
-      nkey[0] = 1ull;
-      nrange[0] = make_int2(0, n);
-      s_rng[0] = make_int2(0, n);
+    s_lb[0] = 0;
+    s_lb[1] = n > 0 ? 1 : 0;
+    for (int d = 1; d <= kMaxDepth; ++d) s_lb[d + 1] = s_lb[d] + totals[d - 1];
+  }
+  warp_start_counts((int)lo, (int)hi, s_first);
+  __syncthreads();
+  if (t < kMaxDepth) {
+    uint32_t run = (uint32_t)s_lb[t + 1] + tile_excl[(size_t)t * ntiles + blockIdx.x];
+    for (int q = 0; q < kPBWarps; ++q) {
+      const uint32_t v = s_first[t][q];
+      s_first[t][q] = run;
+      run += v;
     }
   }
   __syncthreads();
-  for (int d = 0; d < kLevels; ++d) {
-    const int lo = s_bounds[d], hi = s_bounds[d + 1];
-    const int shift = 3 * (kMaxDepth - 1 - d);
-    const int2* cur = s_rng + (d & 1) * n;  // this level's ranges, by node - lo
-    int2* nxt = s_rng + ((d + 1) & 1) * n;  // the next level's, by node - hi
-    int next = hi;                          // index of the next child of this level
-    if (hi > lo && !s_full) {
-      for (int base = lo; base < hi; base += kBuildSmallThreads) {
-        const int node = base + t;
-        const bool valid = node < hi;
-        int2 r = make_int2(0, 0);
-        int bnd[9];
-        int nc = 0;
-        uint32_t mask = 0;
-        bool internal = false;
-        if (valid) {
-          r = cur[node - lo];
-          internal = r.y > leaf_cap && d < kMaxDepth;
-          if (internal) {
-            bnd[0] = r.x;
-            bnd[8] = r.x + r.y;
-            split_search<1, 4>(s_key, shift, bnd);
-            split_search<2, 2>(s_key, shift, bnd);
-            split_search<4, 1>(s_key, shift, bnd);
-            for (int v = 0; v < 8; ++v)
-              if (bnd[v + 1] > bnd[v]) {
-                ++nc;
-                mask |= 1u << v;
-              }
-          }
-        }
-        // block exclusive scan of the child counts
-        uint32_t x = (uint32_t)nc;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-          if (lane >= o) x += y;
-        }
-        if (lane == 31) s_wex[w] = x;
-        __syncthreads();
-        if (w == 0) {
-          const uint32_t v = s_wex[lane];
-          uint32_t z = v;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, z, o);
-            if (lane >= o) z += y;
-          }
-          s_wex[lane] = z - v;
-          if (lane == 31) s_total = z;
-        }
-        __syncthreads();
-        const long long child_base = (long long)next + (x - (uint32_t)nc + s_wex[w]);
-        if (valid) {
-          const bool fits = child_base + nc <= node_cap;
-          if (!fits) {
-            atomicOr(err, kErrNodes);
-            s_full = 1;
-          }
-          const bool make = internal && fits;
-          if (make) {
-            const uint64_t pk = s_key[r.x] >> (3 * (kMaxDepth - d));  // this node's key
-            int k = 0;
-            for (int v = 0; v < 8; ++v) {
-              if (!(mask & (1u << v))) continue;
-              const int ci = (int)child_base + k++;
-              const int2 cr = make_int2(bnd[v], bnd[v + 1] - bnd[v]);
-              nkey[ci] = (pk << 3) | (uint64_t)v;
-              nrange[ci] = cr;
-              nxt[ci - hi] = cr;  // ci - hi < n: a level has at most n nodes
-            }
-          }
-          wn[node].link = make_int4(make ? (int)child_base : -1, make ? nc : 0, r.x, r.y);
-          childbyte[node] = (uint8_t)(make ? mask : 0u);
-        }
-        next += (int)s_total;
-        __syncthreads();  // s_wex and s_total are reused; this tile's children are complete
-      }
-    }
-    if (t == 0) s_bounds[d + 2] = next;
-    __syncthreads();
+  return s_lb[kLevels];
+}
+
+// Node records from the thread of each node's first body: key, first body, parent, first
+// child (node (d + 1, i); a node is internal exactly when d < the body's deepest start depth).
+// The body counts, child counts and child bytes follow in k_nodes_link.
+__global__ __launch_bounds__(kPBThreads) void k_nodes_write(const uint64_t* __restrict__ tkey, int n, int leaf_cap,
+                                                            const uint32_t* __restrict__ span,
+                                                            const uint32_t* __restrict__ tile_excl, int ntiles,
+                                                            const uint32_t* __restrict__ totals,
+                                                            uint64_t* __restrict__ nkey, int2* __restrict__ nrange,
+                                                            WalkNode* __restrict__ wn, uint8_t* __restrict__ childbyte,
+                                                            int* __restrict__ nparent, int* __restrict__ level_bounds,
+                                                            long long node_cap, uint32_t* __restrict__ err) {
+  __shared__ long long s_lb[kLevels + 1];
+  __shared__ uint32_t s_first[kMaxDepth][kPBWarps];
+  const int t = threadIdx.x, lane = t & 31;
+  const int i = blockIdx.x * kPBThreads + t;
+  const uint32_t sp = i < n ? span[i] : 1u;
+  const int lo = (int)(sp & 0xFFu), hi = (int)(sp >> 8);
+  const long long m = node_first_indices(n, (uint32_t)lo, (uint32_t)hi, tile_excl, ntiles, totals, s_lb, s_first);
+  if (blockIdx.x == 0) {
+    if (t <= kLevels + 1) level_bounds[t] = (int)min(s_lb[min(t, kLevels)], 0x7fffffffll);
+    if (t == 0 && m > node_cap) atomicOr(err, kErrNodes);
   }
-  if (t <= kLevels + 1) level_bounds[t] = s_bounds[t];
+  if (m > node_cap) return;  // the host grows the arena and builds again
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint64_t ki = i < n ? tkey[i] : 0ull;
+  int child = -1;  // index of node (d + 1, i), when it exists
+  // the warp's depths, and one above them for the parents of its shallowest nodes
+  const int wlo = __reduce_min_sync(0xffffffffu, lo), whi = __reduce_max_sync(0xffffffffu, hi);
+  for (int d = whi; d >= max(1, wlo - 1); --d) {
+    const bool f = lo <= d && d <= hi;
+    const unsigned b = __ballot_sync(0xffffffffu, f);
+    const int idx = (int)s_first[d - 1][t >> 5] + __popc(b & lt);  // node (d, i) if f, else the next start
+    if (child >= 0) nparent[child] = idx + (f ? 1 : 0) - 1;  // the last depth-d node starting at or before i
+    if (f) {
+      nkey[idx] = ki >> (3 * (kMaxDepth - d));
+      nrange[idx] = make_int2(i, 0);
+      wn[idx].link = make_int4(d < hi ? child : -1, 0, i, 0);
+      childbyte[idx] = 0;
+      child = idx;
+    } else {
+      child = -1;
+    }
+  }
+  if (child >= 0) nparent[child] = 0;  // depth-1 nodes hang from the root
+  if (i == 0) {
+    const bool internal = n > leaf_cap;
+    nkey[0] = 1ull;
+    nrange[0] = make_int2(0, n);
+    wn[0].link = make_int4(internal ? 1 : -1, 0, 0, n);
+    childbyte[0] = 0;
+    nparent[0] = -1;
+  }
+}
+
+// Body counts, child counts and child bytes, one thread per node. Siblings are contiguous and
+// their cells adjacent, so a node's cell ends where its next sibling's starts, and a last
+// child's where its parent's ends (the climb passes only through last children: about 1.3
+// nodes on average). The last child of each parent (the next node has another parent) also
+// counts its siblings from the parent's first child and ORs their digits.
+__global__ __launch_bounds__(kThreads) void k_nodes_link(const int* __restrict__ level_bounds,
+                                                         const uint64_t* __restrict__ nkey,
+                                                         const int* __restrict__ nparent, int2* __restrict__ nrange,
+                                                         WalkNode* __restrict__ wn, uint8_t* __restrict__ childbyte,
+                                                         const uint32_t* __restrict__ err) {
+  if (*err & kErrNodes) return;
+  const int m = level_bounds[kLevels];
+  const int n = nrange[0].y;
+  auto last_child = [&](int j) { return j + 1 >= m || nparent[j + 1] != nparent[j]; };
+  for (int j = 1 + blockIdx.x * kThreads + threadIdx.x; j < m; j += gridDim.x * kThreads) {
+    const bool last = last_child(j);
+    int a = j;
+    bool up = last;
+    while (up) {
+      a = nparent[a];
+      if (a == 0) break;
+      up = last_child(a);
+    }
+    const int first = nrange[j].x;
+    const int cnt = (up ? n : nrange[a + 1].x) - first;  // up: the climb reached the root
+    nrange[j].y = cnt;
+    wn[j].link.w = cnt;
+    if (!last) continue;
+    const int p = nparent[j];
+    const int fc = wn[p].link.x;
+    uint32_t mask = 0;
+    for (int c = fc; c <= j; ++c) mask |= 1u << (uint32_t)(nkey[c] & 7ull);
+    wn[p].link.y = j - fc + 1;
+    childbyte[p] = (uint8_t)mask;
+  }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1285,18 +1402,27 @@ void launch_gather_tree(bh_ctx* c, const uint32_t* tslot, int n, const float4* p
   if (n > 0) k_gather_tree<<<grid_for(n), kThreads, 0, c->stream>>>(tslot, n, pos, tpos);
 }
 
-// Function attributes set once per process, before any stream capture.
-void tree_init() {
-  cudaFuncSetAttribute(k_build_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBuildSmallSmem);
-}
+// Function attributes set once per process, before any stream capture (none at present).
+void tree_init() {}
 
 void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
-  if (!batch && n <= kBuildSmallMax) {
-    c->launches += 1;
-    const size_t smem = (sizeof(uint64_t) + 2 * sizeof(int2)) * (size_t)n;  // <= kBuildSmallSmem
-    k_build_small<<<1, kBuildSmallThreads, smem, c->stream>>>(
-        n, c->tkey, leaf_cap, c->nkey, c->nrange, c->wnode, c->nchildbyte, c->level_bounds, (long long)c->node_cap,
-        c->err);
+  if (!batch && n >= 1 && leaf_cap <= kPBMaxLeaf) {
+    // every depth at once: counts per tile and depth (in lb_level), their scans (totals in
+    // level_tile_ctr), the node records (start depths of each body in vals[1], free after the
+    // sorts), then child counts and bytes
+    const int ntiles = (n + kPBThreads - 1) / kPBThreads;
+    uint32_t* span = c->vals[1];
+    uint32_t* tile = c->lb_level;
+    uint32_t* totals = c->level_tile_ctr;
+    c->launches += 4;
+    k_nodes_count<<<ntiles, kPBThreads, 0, c->stream>>>(c->tkey, n, leaf_cap, span, tile, ntiles);
+    k_nodes_scan<<<kMaxDepth, 1024, 0, c->stream>>>(tile, ntiles, totals);
+    k_nodes_write<<<ntiles, kPBThreads, 0, c->stream>>>(c->tkey, n, leaf_cap, span, tile, ntiles, totals, c->nkey,
+                                                        c->nrange, c->wnode, c->nchildbyte, c->nparent,
+                                                        c->level_bounds, (long long)c->node_cap, c->err);
+    const int lgrid = (int)std::min<size_t>(152 * 8, (c->node_cap + kThreads - 1) / kThreads);
+    k_nodes_link<<<lgrid, kThreads, 0, c->stream>>>(c->level_bounds, c->nkey, c->nparent, c->nrange, c->wnode,
+                                                    c->nchildbyte, c->err);
     return;
   }
   c->launches += 1 + kLevels;

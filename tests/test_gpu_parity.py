@@ -167,8 +167,8 @@ def test_coincident_bodies_bucket_at_depth21(bh, orc, sim):
     assert np.all(np.isfinite(acc))
 
 
-# the sorts go by rank up to 16 384 keys and the build runs in one block up to 8 192 bodies;
-# the sizes either side of both limits take both paths
+# the sorts go by rank up to 16 384 keys (the radix sort beyond): the sizes either side of the
+# limit take both paths
 @pytest.mark.parametrize("n", [1, 2, 3, 31, 32, 33, 1000, 1025, 4097, 8192, 8193, 16384, 16385])
 def test_small_and_ragged_n(bh, orc, sim, n):
     pm, v = bh.plummer(300 + n, n)
@@ -211,6 +211,30 @@ def test_node_lookup(bh, sim):
     with pytest.raises(bh.BHError) as e:
         sim.lookup((1 << 60) | 12345)
     assert e.value.code == 9
+
+
+@pytest.mark.parametrize("leaf", [1, 8, 64, 65, 200])
+def test_build_paths_by_leaf_capacity(bh, orc, sim, leaf):
+    """Leaf capacities up to 64 build every depth at once, larger ones level by level; both give
+    the reference's node set, counts and child bytes."""
+    n = 20000
+    pm, v = bh.plummer(77, n)
+    pm[5000:5040, :3] = pm[11, :3]  # a run of coincident bodies: a bucket at depth 21
+    sim.set_bodies(pm, v)
+    c, size = sim.bounds()
+    sim.morton_keys(size)
+    perm = sim.sort_bodies()
+    sp = pm[perm]
+    pos, mass = sp[:, :3].astype(np.float64), sp[:, 3].astype(np.float64)
+    sim.build(c, 2 * size, leaf, bh.BH_MULTIPOLE_QUADRUPOLE)
+    t = sim.tree_nodes()
+    ref_t = orc.build(pos, mass, c, 2 * size, leaf, 1)
+    assert np.array_equal(t["keys"], ref_t["keys"])
+    assert np.array_equal(t["counts"], ref_t["counts"])
+    assert np.array_equal(t["child_byte"], ref_t["child_byte"])
+    acc = sim.force(0.5, 0.01)
+    ref_acc, _, _ = orc.force(pos, mass, c, 2 * size, leaf, 1, 0.5, 0.01, nthreads=8)
+    assert_acc_close(acc, ref_acc)
 
 
 def test_node_arena_growth(bh, orc, sim):
