@@ -558,7 +558,7 @@ def run_ensemble(args, dist):
             launches += st.kernel_launches
             per_step.append(st.ms_step)
             walk_ms.append(st.ms_walk)
-            flops.append(FLOPS_P2P * st.interactions_p2p + cell_flops * st.interactions_cell)
+            flops.append(FLOPS_P2P * st.interactions_p2p + FLOPS_CELL_QUAD * st.interactions_cell)
             for key, val in st.as_dict().items():
                 if key.startswith("ms_"):
                     stage[key] = stage.get(key, 0.0) + val
