@@ -395,6 +395,8 @@ __global__ __launch_bounds__(kThreads) void k_gather_tree(const uint32_t* __rest
 // The node set equals the reference's insertion result: the root, plus every prefix K of a
 // body's depth-21 path whose parent holds more than leaf_cap bodies (for leaf capacity 1:
 // count(parent) >= 2). Bodies are sorted by path, so every node is a contiguous body range.
+// Two builds produce the same records: the all-depths build further down (single systems with
+// leaf capacity up to 64), and this level build (ensembles, larger leaf capacities).
 // One launch per depth turns the internal nodes of depth d into the node records of depth
 // d+1, appended in key order: children get contiguous indices, depths are stored level by
 // level (breadth-first), and a decoupled look-back over 256-node tiles assigns the indices.
