@@ -136,11 +136,11 @@ def test_reset_same_count_replays_identically(bh):
             assert np.array_equal(g, r)
 
 
-def test_step_host_matches_step(bh):
+@pytest.mark.parametrize("n", [5000, 70000])
+def test_step_host_matches_step(bh, n):
     """bh_step_host (upload, step, download; copies overlapped with page-locked buffers) follows
     the same trajectory as bh_step, bit for bit: with page-locked buffers, with buffers that
     change between calls (re-capture), with pageable numpy arrays, and with no copies at all."""
-    n = 5000
     pm, vel = bh.plummer(8, n)
     prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1, edge_factor=2.0)
     steps = 6
