@@ -65,3 +65,20 @@ def test_bench_functions_read_only_defined_names():
             if isinstance(node, ast.Name) and isinstance(node.ctx, ast.Load) and node.id not in bound:
                 missing.append(f"{fn.name}:{node.lineno}: {node.id}")
     assert not missing, missing
+
+
+def test_reference_arm_on_the_app_frame():
+    """`bench.py --impl reference --workload app-solar-4444` runs on the CPU alone: the app's
+    scene from the oracle's restatement of its generator, the literal walk, one JSON line."""
+    import json
+    import subprocess
+    import sys
+
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
+                          "app-solar-4444", "--steps", "1", "--warmup", "3"],
+                         capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    d = json.loads(out.stdout.strip().splitlines()[-1])
+    assert d["impl"] == "reference" and d["value"] > 0
+    assert d["config"]["workload"] == "app-solar-4444" and d["config"]["bodies"] == 4444
+    assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
