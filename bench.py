@@ -15,12 +15,15 @@ upsweep, walk + force, kick.
          overlapped with the step on a second stream; CUDA events around the whole call.
   roofline  the tree walk (the dominant kernel) against the measured FP32 FMA peak of this GPU
          (bh_measure_fp32_peak); the Morton sort against MEASURED_PEAKS.json's HBM copy peak.
-  cpu_baseline  the oracle port of the reference's serial path on this host's cores (1 thread,
-         as the reference), on a bounded sample: the full tree build over all N bodies plus the
-         walk of a seeded subsample, extrapolated to N (stated in "sample").
+  cpu_baseline  the oracle port of the reference's step on this host: one whole step of the same
+         workload (every body walked) with all host threads; cpu_serial: whole steps of the
+         N = 16 384 configuration on one thread, as the reference runs.
+  ensemble / adjoint  the batched and reverse-mode halves of the metric, measured in the same run
+         (the ensemble-4096 and adjoint-64k workloads, 5 timed steps each; --no-modes skips them).
 
 --impl reference: the reference's CPU implementation of the same step (the oracle port: the
-reference's own sources cannot be compiled on this machine), with all host threads.
+reference's own sources cannot be compiled on this machine), W + K whole steps with all host
+threads, the K steps timed.
 Multi-GPU (torchrun): independent replicas, one per GPU (the single-system step does not
 shard); value = sum of per-rank body-steps / max-over-ranks time.
 """
@@ -70,6 +73,8 @@ METRIC = "body-steps/s @theta=0.5, acc err<=1e-3: plain vs batched/adjoint, 1 GB
 # d.Q.d 5, scale 2, update 7)
 FLOPS_P2P, FLOPS_CELL_QUAD = 20, 57
 SORT_PASSES = 8
+# steps of the ensemble and adjoint figures carried in the default workload's line
+MODE_STEPS, MODE_WARMUP = 5, 3
 
 
 def log(*a):
@@ -98,11 +103,9 @@ class Dist:
         return self.local if self.ws > 1 else 0
 
     def simulation(self, bh, n):
-        """A context on this rank's GPU (device 0 when the rank's GPU is the only visible one)."""
-        try:
-            return bh.Simulation(n, device=self.device())
-        except bh.BHError:
-            return bh.Simulation(n, device=0)
+        """A context on this rank's GPU. A rank whose GPU cannot be opened fails (a replica never
+        moves onto another rank's GPU)."""
+        return bh.Simulation(n, device=self.device())
 
     def gpu_index(self):
         """nvidia-smi index of this rank's GPU (BH_GPU_INDEX overrides)."""
@@ -276,32 +279,57 @@ def accuracy_vs_direct(w, pm, acc_by_theta, orc, nthreads, ntarget=4096, ntarget
     return res
 
 
-def cpu_sample(bh, w, pm, nthreads, walk_sample):
-    """Oracle port of one reference step on a bounded sample: bounds, keys, sort, kick+drift and
-    the tree build run on all N bodies; the walk runs on a seeded subsample and is scaled to N."""
+def cpu_whole_steps(bh, w, pm, vel, nthreads, nsteps, acc=None):
+    """The oracle port of the reference's per-frame step (bounds, Morton keys, sort, kick+drift,
+    tree build, walk + force over every body, kick; src/ofApp.cpp:169-177, 248-282), nsteps whole
+    steps from (pm, vel) with nthreads walk threads (the rest of the step is serial, as in the
+    reference). Returns the end state and the wall seconds of the call."""
     from oracle.oracle import Restatement
 
     orc = Restatement()
-    n = len(pm)
     pos = pm[:, :3].astype(np.float64)
-    mass = pm[:, 3].astype(np.float64)
+    v = vel[:, :3].astype(np.float64)
+    m = pm[:, 3].astype(np.float64)
+    a = np.zeros_like(pos) if acc is None else acc
     t0 = time.perf_counter()
-    c, size = orc.bounds(pos)
-    keys = orc.morton_keys(pos, size)
-    perm = orc.sort_perm(keys)
-    sp, sm = pos[perm], mass[perm]
-    t1 = time.perf_counter()
-    rng = np.random.default_rng(99)
-    tgt = np.sort(rng.choice(n, min(walk_sample, n), replace=False)).astype(np.uint32)
-    build_s, walk_s, _ = orc.time_sample(sp, sm, c, size * w["edge"], w["leaf"], multipole_mode(bh, w)[1],
-                                         w["theta"], w["eps"], tgt, nthreads=nthreads)
-    fixed = (t1 - t0) + build_s
-    per_step = fixed + walk_s * n / len(tgt)
-    return {"value": n / per_step, "unit": "body-steps/s", "cores": nthreads, "kind": "port",
-            "sample": (f"bounds+keys+sort on all {n} bodies ({t1 - t0:.3g} s) + tree build on all {n} "
-                       f"({build_s:.3g} s) + walk of {len(tgt)} sampled bodies ({walk_s:.3g} s) scaled to {n}; "
-                       f"{nthreads} thread(s); extrapolated step {per_step:.3g} s"),
-            "seconds_per_step": per_step}
+    r = orc.steps(pos, v, m, a, w["dt"], w["theta"], w["eps"], w["edge"], w["leaf"], multipole_mode(bh, w)[1],
+                  nsteps, acc_follows_body=w.get("acc_follows_body", 1), nthreads=nthreads)
+    r["wall_s"] = time.perf_counter() - t0
+    return r
+
+
+def cpu_state(r):
+    """(pos_m, vel) float32 arrays of an oracle end state (the next call's start)."""
+    pm = np.zeros((len(r["pos"]), 4), np.float32)
+    vel = np.zeros_like(pm)
+    pm[:, :3], pm[:, 3], vel[:, :3] = r["pos"], r["mass"], r["vel"]
+    return pm, vel
+
+
+STAGE_NAMES = ("bounds_keys", "sort_reorder", "kick_drift", "build", "walk_force", "kick")
+
+
+def cpu_baseline_whole_step(bh, w, pm, vel, nthreads):
+    """cpu_baseline: one whole step of the same workload (every body walked) by the oracle port
+    on nthreads host threads; no sampling, no extrapolation."""
+    r = cpu_whole_steps(bh, w, pm, vel, nthreads, 1)
+    n = len(pm)
+    return {"value": n / r["wall_s"], "unit": "body-steps/s", "cores": nthreads, "kind": "port",
+            "sample": (f"1 whole step of the same workload ({n} bodies, every body walked) by the oracle port on "
+                       f"{nthreads} host thread(s) (walk threaded, the rest serial): {r['wall_s']:.3g} s"),
+            "stage_s": dict(zip(STAGE_NAMES, (float(x) for x in r["stage_s"])))}
+
+
+def cpu_serial_config0(bh, nsteps=10):
+    """The serial figure: whole steps of the small Plummer configuration (N = 16 384, theta 0.5,
+    eps 0.01, leaf 1, dt 1e-3) by the oracle port on one thread, as the reference runs."""
+    w = WORKLOADS["plummer-16k"]
+    pm, vel = make_inputs(bh, w, w["seed"])
+    r = cpu_whole_steps(bh, w, pm, vel, 1, nsteps)
+    return {"value": w["n"] * nsteps / r["wall_s"], "unit": "body-steps/s", "cores": 1, "kind": "port",
+            "workload": "plummer-16k", "steps": nsteps, "seconds_per_step": r["wall_s"] / nsteps,
+            "sample": f"{nsteps} whole steps of the N=16384 Plummer configuration (theta 0.5, eps 0.01, leaf 1), "
+                      f"1 thread"}
 
 
 def cpu_steps_sample(systems, theta, eps, dt, leaf, edge, nthreads=1):
@@ -320,34 +348,43 @@ def cpu_steps_sample(systems, theta, eps, dt, leaf, edge, nthreads=1):
     return out
 
 
+def workload_config(args, w):
+    """The `config` object of a workload line; both arms print the same one."""
+    return {"workload": args.workload, "bodies": w["n"], "desc": w["desc"]}
+
+
 def run_reference(args, w, dist):
-    """CPU reference arm: the oracle port of the reference's step with all host threads."""
+    """CPU reference arm: the oracle port of the reference's step, whole steps on every body, with
+    all host threads: W untimed warm-up steps, then K timed steps continuing the same trajectory.
+    Under torchrun only rank 0 runs."""
     if dist.rank != 0:
         return
     import __graft_entry__
 
     bh = __graft_entry__.package()
-    pm, _ = make_inputs(bh, w, w["seed"])
+    pm, vel = make_inputs(bh, w, w["seed"])
     nthreads = os.cpu_count() or 1
-    sample = 65536
-    for _ in range(args.warmup):
-        pass  # a CPU step has no warm-up state; warm-up steps are not repeated
-    vals = []
-    t_all = time.perf_counter()
-    for k in range(args.steps):
-        r = cpu_sample(bh, w, pm, nthreads, sample)
-        vals.append(r["seconds_per_step"])
-    wall = time.perf_counter() - t_all
-    per_step = statistics.mean(vals)
-    value = w["n"] / per_step
+    acc = None
+    if args.warmup > 0:
+        r = cpu_whole_steps(bh, w, pm, vel, nthreads, args.warmup)
+        pm, vel = cpu_state(r)
+        acc = r["acc"]
+    r = cpu_whole_steps(bh, w, pm, vel, nthreads, args.steps, acc=acc)
+    wall = r["wall_s"]
+    value = w["n"] * args.steps / wall
+    sample = (f"{args.steps} whole steps of the workload ({w['n']} bodies, every body walked) by the oracle port "
+              f"on {nthreads} host threads (walk threaded, the rest serial), after {args.warmup} untimed warm-up "
+              f"steps: {wall:.3g} s")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "bodies": w["n"], "desc": w["desc"]},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args, w),
+            "timing": "wall clock around the K timed steps (one call into the oracle port)",
             "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": nthreads, "kind": "port",
-                             "sample": r["sample"]},
+                             "sample": sample},
             "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "wall_s": wall}
+            "stage_s_per_step": {k: float(x) / args.steps for k, x in zip(STAGE_NAMES, r["stage_s"])},
+            "steps_timed": args.steps, "wall_s": wall}
     print(json.dumps(line), flush=True)
 
 
@@ -469,9 +506,9 @@ def run_ours(args, w, dist):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (keys, bounds, tree geometry and upsweep in f64)",
         "data": "synthetic", "impl": "ours",
-        "config": {"workload": args.workload, "bodies": n, "desc": w["desc"],
-                   "timing": "per-step CUDA events on the library stream; L2 flushed between steps",
-                   "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"},
+        "config": workload_config(args, w),
+        "timing": "per-step CUDA events on the library stream; L2 flushed between steps",
+        "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
                 "ms_per_step": statistics.median(e2e_ms)},
         "interactions_per_s": dist.sum(sum(inter)) / (total_ms * 1e-3),
@@ -508,13 +545,19 @@ def run_ours(args, w, dist):
         "autotune": tune,
     }
     if dist.rank == 0:
-        clk = clocks.summary()
-        line["clocks"] = clk
-        if dist.ws == 1 and not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_sample(bh, w, pm, 1, args.cpu_walk_sample)
-            line["cpu_baseline"].pop("seconds_per_step", None)
-        print(json.dumps(line), flush=True)
+        line["clocks"] = clocks.summary()
     sim.close()
+    if args.workload == "plummer-4m" and not args.no_modes:
+        # the batched and reverse-mode halves of the metric, measured in the same run
+        line["ensemble"] = ensemble_summary(measure_ensemble(bh, dist, MODE_STEPS, MODE_WARMUP, args.loop_sample,
+                                                             with_cpu=False))
+        line["adjoint"] = adjoint_summary(measure_adjoint(bh, dist, MODE_STEPS, MODE_WARMUP, with_cpu=False))
+    if dist.rank == 0:
+        if dist.ws == 1 and not args.no_cpu_baseline:
+            nthreads = os.cpu_count() or 1
+            line["cpu_baseline"] = cpu_baseline_whole_step(bh, w, pm, vel, nthreads)
+            line["cpu_serial"] = cpu_serial_config0(bh)
+        print(json.dumps(line), flush=True)
 
 
 ENSEMBLE = dict(nsys=4096, nmin=256, nmax=65536, theta=0.6, eps=0.01, leaf=8, dt=1e-3, edge=2.0, seed=1000,
@@ -522,14 +565,11 @@ ENSEMBLE = dict(nsys=4096, nmin=256, nmax=65536, theta=0.6, eps=0.01, leaf=8, dt
                      "in [256, 65536], M = a = 1 each, theta=0.6, eps=0.01, leaf 8, dt=1e-3, quadrupole, edge 2S")
 
 
-def run_ensemble(args, dist):
+def measure_ensemble(bh, dist, steps, warmup, loop_sample, with_cpu):
     """Batched ensemble: all systems in one bh_batch_step per step (graph-replayed), against the
     plain path looped over the systems (each system resident in its own context, one bh_step
-    call per system per step, wall-clock), estimated from a seeded sample of systems."""
-    import __graft_entry__
-
-    bh = __graft_entry__.package()
-    bh.load()
+    call per system per step, wall-clock), estimated from a seeded sample of systems. Returns the
+    workload's JSON line (every rank; rank 0 prints it)."""
     e = ENSEMBLE
     rng = np.random.default_rng(e["seed"])
     u = rng.uniform(0.0, 1.0, e["nsys"])
@@ -545,14 +585,14 @@ def run_ensemble(args, dist):
     fp32_peak = sim.fp32_peak_tflops()
     sim.batch_step(prm, 1, stats=False)
     tune = sim.autotune(e["theta"], e["eps"], trials=2)  # walk launch shape for this ensemble
-    for _ in range(args.warmup - 1):  # re-captures the step graph with the chosen walk
+    for _ in range(warmup - 1):  # re-captures the step graph with the chosen walk
         sim.batch_step(prm, 1, stats=False)
     per_step, flops, walk_ms = [], [], []
     stage = {}
     launches = 0
     dist.barrier()
     with ClockSampler(dist.gpu_index()) as clocks:
-        for _ in range(args.steps):
+        for _ in range(steps):
             sim.flush_l2()
             st = sim.batch_step(prm, 1)
             launches += st.kernel_launches
@@ -563,7 +603,7 @@ def run_ensemble(args, dist):
                 if key.startswith("ms_"):
                     stage[key] = stage.get(key, 0.0) + val
     total_ms = dist.max(sum(per_step))
-    value = dist.sum(n * args.steps) / (total_ms * 1e-3)
+    value = dist.sum(n * steps) / (total_ms * 1e-3)
     # end to end: bh_batch_step_host uploads every system's positions and velocities from pinned
     # host memory, steps the ensemble and downloads them, its copies beside the step (one call
     # captures; the timed calls replay)
@@ -584,7 +624,7 @@ def run_ensemble(args, dist):
     sim.close()
     # the plain path looped over the systems, on a seeded sample of systems
     rng = np.random.default_rng(7)
-    sample = np.sort(rng.choice(e["nsys"], args.loop_sample, replace=False))
+    sample = np.sort(rng.choice(e["nsys"], loop_sample, replace=False))
     loop_s = []
     for s in sample:
         a, b = int(off[s]), int(off[s + 1])
@@ -602,7 +642,7 @@ def run_ensemble(args, dist):
     walk_tflops = statistics.mean(flops) / (statistics.mean(per_step) * 1e-3) / 1e12
     walk_only_tflops = statistics.mean(flops) / (statistics.mean(walk_ms) * 1e-3) / 1e12 if min(walk_ms) > 0 else None
     cpu = None
-    if dist.rank == 0 and not args.no_cpu_baseline:
+    if dist.rank == 0 and with_cpu:
         # the oracle port on one core over 12 seeded systems, scaled by sum N log N
         sizes = np.diff(off).astype(np.float64)
         pick = np.sort(np.random.default_rng(8).choice(e["nsys"], 12, replace=False))
@@ -614,31 +654,52 @@ def run_ensemble(args, dist):
                "sample": f"one oracle-port step of 12 seeded systems ({sum(secs):.1f} s, "
                          f"{int(sizes[pick].sum())} bodies), scaled by sum N log N to all {e['nsys']} systems: "
                          f"{cpu_step_s:.0f} s per ensemble step"}
+    line = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": dist.ws, "steps": steps,
+            "warmup": warmup, "ms_per_step": total_ms / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "ours",
+            "config": {"workload": "ensemble-4096", "systems": e["nsys"], "bodies": n, "desc": e["desc"]},
+            "timing": "per-step CUDA events inside the captured step; L2 flushed between steps",
+            "e2e": {"value": n / (statistics.median(e2e) * 1e-3), "unit": "body-steps/s",
+                    "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
+                    "ms_per_step": statistics.median(e2e)},
+            "plain_loop": {"value": n / loop_step_s, "unit": "body-steps/s", "seconds_per_step": loop_step_s,
+                           "sample": f"{len(sample)} seeded systems, each in its own context, wall-clock bh_step "
+                                     f"(median of 3), sum scaled by {e['nsys']}/{len(sample)}"},
+            "batched_speedup_vs_plain_loop": loop_step_s / (total_ms / steps * 1e-3),
+            "flops_per_step": statistics.mean(flops), "tflops": walk_tflops,
+            "fp32_peak_tflops": fp32_peak, "gpu_launches": launches, "autotune": tune,
+            "roofline": {"kernel": "k_walk<quadrupole> (ensemble groups)", "bound": "fp32",
+                         "achieved": walk_only_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": (walk_only_tflops / fp32_peak) if walk_only_tflops and fp32_peak else None,
+                         "peak_source": "measured FP32 FMA peak of this GPU (bh_measure_fp32_peak)",
+                         "traffic": None, "flops_per_launch": statistics.mean(flops),
+                         "ms_per_launch": statistics.mean(walk_ms)},
+            "stage_ms_per_step": {k[3:]: v / steps for k, v in stage.items()},
+            "clocks": clocks.summary()}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    return line
+
+
+def ensemble_summary(line):
+    """The ensemble figures carried in the headline line."""
+    keys = ("value", "unit", "ms_per_step", "steps", "warmup", "batched_speedup_vs_plain_loop", "gpu_launches")
+    out = {k: line[k] for k in keys}
+    out["plain_loop_ms_per_step"] = line["plain_loop"]["seconds_per_step"] * 1e3
+    out["plain_loop_sample"] = line["plain_loop"]["sample"]
+    out["e2e"] = line["e2e"]
+    out["config"] = line["config"]
+    out["walk_frac"] = line["roofline"]["frac"]
+    return out
+
+
+def run_ensemble(args, dist):
+    import __graft_entry__
+
+    bh = __graft_entry__.package()
+    bh.load()
+    line = measure_ensemble(bh, dist, args.steps, args.warmup, args.loop_sample, not args.no_cpu_baseline)
     if dist.rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "ours",
-                "config": {"workload": "ensemble-4096", "systems": e["nsys"], "bodies": n, "desc": e["desc"],
-                           "timing": "per-step CUDA events inside the captured step; L2 flushed between steps"},
-                "e2e": {"value": n / (statistics.median(e2e) * 1e-3), "unit": "body-steps/s",
-                        "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
-                        "ms_per_step": statistics.median(e2e)},
-                "plain_loop": {"value": n / loop_step_s, "unit": "body-steps/s", "seconds_per_step": loop_step_s,
-                               "sample": f"{len(sample)} seeded systems, each in its own context, wall-clock bh_step "
-                                         f"(median of 3), sum scaled by {e['nsys']}/{len(sample)}"},
-                "batched_speedup_vs_plain_loop": loop_step_s / (total_ms / args.steps * 1e-3),
-                "flops_per_step": statistics.mean(flops), "tflops": walk_tflops,
-                "fp32_peak_tflops": fp32_peak, "gpu_launches": launches, "autotune": tune,
-                "roofline": {"kernel": "k_walk<quadrupole> (ensemble groups)", "bound": "fp32",
-                             "achieved": walk_only_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                             "frac": (walk_only_tflops / fp32_peak) if walk_only_tflops and fp32_peak else None,
-                             "peak_source": "measured FP32 FMA peak of this GPU (bh_measure_fp32_peak)",
-                             "traffic": None, "flops_per_launch": statistics.mean(flops),
-                             "ms_per_launch": statistics.mean(walk_ms)},
-                "stage_ms_per_step": {k[3:]: v / args.steps for k, v in stage.items()},
-                "clocks": clocks.summary()}
-        if cpu:
-            line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
 
 
@@ -648,15 +709,11 @@ ADJOINT = dict(n=65536, nsteps=200, every=20, theta=0.5, eps=0.01, leaf=8, dt=1e
                     "with lognormal(0.1) mass factors (seed 2); checkpoints every 20 steps")
 
 
-def run_adjoint(args, dist):
+def measure_adjoint(bh, dist, steps, warmup, with_cpu):
     """Reverse mode: a step is one gradient of the loss over the whole 200-step trajectory
     (bh_adjoint_forward with checkpoints + bh_step_backward with recomputation). Beside it, the
     plain forward path (bh_step) over the same 200 steps, so the backward/forward cost ratio is
-    measured in the same run."""
-    import __graft_entry__
-
-    bh = __graft_entry__.package()
-    bh.load()
+    measured in the same run. Returns the workload's JSON line."""
     a = ADJOINT
     n, ns = a["n"], a["nsteps"]
     pm, vel = bh.plummer(a["seed"], n)
@@ -681,24 +738,24 @@ def run_adjoint(args, dist):
         g = sim.step_backward(dl, None, stats=True)
         return f, g[3], float(np.mean(np.sum((p[:, :3] - target) ** 2, axis=1)))
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         gradient(False)
     fwd, bwd, launches = [], [], 0
     dist.barrier()
     with ClockSampler(dist.gpu_index()) as clocks:
-        for _ in range(args.steps):
+        for _ in range(steps):
             f, b, loss = gradient(True)
             fwd.append(f.ms_step)
             bwd.append(b.ms_step)
             launches += f.kernel_launches + b.kernel_launches
         # the plain forward path over the same trajectory length
         plain = []
-        for _ in range(max(2, args.steps)):
+        for _ in range(max(2, steps)):
             sim.set_bodies(pm, vel)
             sim.flush_l2()
             plain.append(sim.step(prm, ns).ms_step)
     total_ms = dist.max(sum(fwd) + sum(bwd))
-    value = dist.sum(n * ns * args.steps) / (total_ms * 1e-3)
+    value = dist.sum(n * ns * steps) / (total_ms * 1e-3)
     # end to end through the C ABI: host state in, loss cotangent in, gradients out
     pp, pv, pd = bh.PinnedArray((n, 4)), bh.PinnedArray((n, 4)), bh.PinnedArray((n, 4))
     pp.array[:] = pm
@@ -718,34 +775,50 @@ def run_adjoint(args, dist):
     sim.close()
     plain_ms = statistics.median(plain)
     cpu = None
-    if dist.rank == 0 and not args.no_cpu_baseline:
+    if dist.rank == 0 and with_cpu:
         secs = cpu_steps_sample([(pm, vel)] * 2, a["theta"], a["eps"], a["dt"], a["leaf"], a["edge"])
         per = statistics.mean(secs)
         cpu = {"value": n / per, "unit": "body-steps/s (forward only)", "cores": 1, "kind": "port",
                "sample": f"two oracle-port forward steps of the N={n} system ({sum(secs):.1f} s); the reference "
                          f"has no reverse mode, so this is its forward cost per step"}
+    line = {"metric": METRIC, "value": value, "unit": "body-steps/s (differentiated)", "n_gpus": dist.ws,
+            "steps": steps, "warmup": warmup, "ms_per_step": total_ms / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "ours",
+            "config": {"workload": "adjoint-64k", "bodies": n, "kdk_steps": ns, "checkpoint_every": a["every"],
+                       "desc": a["desc"]},
+            "timing": "a step = one gradient over the 200-step trajectory; CUDA events around "
+                      "bh_adjoint_forward and bh_step_backward; L2 flushed before each",
+            "forward_ms": statistics.median(fwd), "backward_ms": statistics.median(bwd),
+            "plain_forward_ms": plain_ms,
+            "backward_over_forward": statistics.median(bwd) / plain_ms,
+            "gradient_over_forward": (statistics.median(fwd) + statistics.median(bwd)) / plain_ms,
+            "loss": loss,
+            "gradient_checks": "tests/test_gpu_adjoint.py (FP64 frozen-list central differences, FP64 "
+                               "direct-sum adjoint)",
+            "e2e": {"value": n * ns / (statistics.median(e2e) * 1e-3), "unit": "body-steps/s (differentiated)",
+                    "h2d_bytes_per_step": 48 * n, "d2h_bytes_per_step": 32 * n + 36 * n,
+                    "ms_per_step": statistics.median(e2e)},
+            "gpu_launches": launches, "clocks": clocks.summary()}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    return line
+
+
+def adjoint_summary(line):
+    """The reverse-mode figures carried in the headline line."""
+    keys = ("value", "unit", "ms_per_step", "steps", "warmup", "forward_ms", "backward_ms", "plain_forward_ms",
+            "backward_over_forward", "gradient_over_forward", "gpu_launches", "e2e", "config")
+    return {k: line[k] for k in keys}
+
+
+def run_adjoint(args, dist):
+    import __graft_entry__
+
+    bh = __graft_entry__.package()
+    bh.load()
+    line = measure_adjoint(bh, dist, args.steps, args.warmup, not args.no_cpu_baseline)
     if dist.rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "body-steps/s (differentiated)", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic", "impl": "ours",
-                "config": {"workload": "adjoint-64k", "bodies": n, "kdk_steps": ns, "checkpoint_every": a["every"],
-                           "desc": a["desc"],
-                           "timing": "a step = one gradient over the 200-step trajectory; CUDA events around "
-                                     "bh_adjoint_forward and bh_step_backward; L2 flushed before each"},
-                "forward_ms": statistics.median(fwd), "backward_ms": statistics.median(bwd),
-                "plain_forward_ms": plain_ms,
-                "backward_over_forward": statistics.median(bwd) / plain_ms,
-                "gradient_over_forward": (statistics.median(fwd) + statistics.median(bwd)) / plain_ms,
-                "loss": loss,
-                "gradient_checks": "tests/test_gpu_adjoint.py (FP64 frozen-list central differences, FP64 "
-                                   "direct-sum adjoint)",
-                "e2e": {"value": n * ns / (statistics.median(e2e) * 1e-3), "unit": "body-steps/s (differentiated)",
-                        "h2d_bytes_per_step": 48 * n, "d2h_bytes_per_step": 32 * n + 36 * n,
-                        "ms_per_step": statistics.median(e2e)},
-                "gpu_launches": launches, "clocks": clocks.summary()}
-        if cpu:
-            line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
 
 
@@ -759,7 +832,8 @@ def main():
                     choices=sorted(WORKLOADS) + ["ensemble-4096", "adjoint-64k"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
-    ap.add_argument("--cpu-walk-sample", type=int, default=16384)
+    ap.add_argument("--no-modes", action="store_true",
+                    help="skip the ensemble and adjoint figures of the default workload's line")
     ap.add_argument("--loop-sample", type=int, default=128)
     args = ap.parse_args()
     if args.warmup < 3:
