@@ -255,10 +255,13 @@ bh_status bh_measure_fp32_peak(bh_ctx* ctx, double* tflops);
  * 64-bit key (the same permutation as bh_sort_bodies) into keys_out / vals_out; the inputs
  * are left unchanged; asynchronous on `stream` (a cudaStream_t, NULL for the legacy default
  * stream) on the current device. status_out (optional, device memory) becomes nonzero if a
- * device-side wait gave up, in which case the output is unspecified.
+ * device-side wait gave up, in which case the output is unspecified; a give-up is reported
+ * only there, so a caller that needs to know of one passes status_out.
  * The first call on each device looks up the scratch array's device address, so make it before
- * any stream capture on that device. Every call reuses the same scratch: calls that can overlap
- * on the GPU (unordered streams, concurrent host threads) race, and the caller must order them. */
+ * any stream capture on that device. The address is kept for the life of the process: after a
+ * cudaDeviceReset (which unloads the library's device code) the entry point must not be called
+ * again on that device. Every call reuses the same scratch: calls that can overlap on the GPU
+ * (unordered streams, concurrent host threads) race, and the caller must order them. */
 #define BH_SORT_STATIC_MAX_KEYS 65536
 bh_status bh_sort_keys_static(const uint64_t* keys_in, const uint32_t* vals_in, uint64_t* keys_out,
                               uint32_t* vals_out, size_t n, void* stream, uint32_t* status_out);

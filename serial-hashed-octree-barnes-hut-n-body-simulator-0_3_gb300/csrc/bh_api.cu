@@ -236,6 +236,11 @@ bh_status bh_create(bh_ctx** out, size_t capacity, int device) {
   if (!c) return BH_ERR_OOM;
   c->device = device;
   c->cap = capacity;
+  if (cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || c->sms <= 0) {
+    cudaGetLastError();
+    delete c;
+    return BH_ERR_DEVICE;
+  }
   auto fail = [&](bh_status s) {
     bh_destroy(c);
     return s;
@@ -268,7 +273,7 @@ bh_status bh_create(bh_ctx** out, size_t capacity, int device) {
   if (s == BH_OK) s = dalloc(&c->level_bounds, kLevels + 2);
   if (s == BH_OK) s = dalloc(&c->level_tile_ctr, kLevels);
   if (s == BH_OK) s = dalloc(&c->geom, 1);
-  c->bounds_blocks = 152 * 2;
+  c->bounds_blocks = c->sms * 2;
   if (s == BH_OK) s = dalloc(&c->bounds_partial, (size_t)c->bounds_blocks * 6);
   if (s == BH_OK) s = dalloc(&c->err, 1);
   if (s == BH_OK) s = dalloc(&c->counters, 1);

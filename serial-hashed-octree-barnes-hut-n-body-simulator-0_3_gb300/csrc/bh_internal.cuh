@@ -113,6 +113,7 @@ struct Arena {
 
 struct bh_ctx {
   int device = 0;
+  int sms = 0;  // streaming multiprocessors of the device (grid sizing)
   size_t cap = 0;  // bodies
   size_t n = 0;
   cudaStream_t stream = nullptr;      // where the context's work runs (own_stream or the caller's)

@@ -346,11 +346,6 @@ void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t*
   *keys_out = keys_in;
   *vals_out = vals_in;
   if (n <= 1) return;
-  static bool attr_set = false;
-  if (!attr_set) {
-    sort_init();
-    attr_set = true;
-  }
   if (n <= kRankSortMax && first_pass == 0 && npasses == kPasses) {
     // the result goes back to keys_in / vals_in, as after the eight digit passes
     c->launches += 2;
@@ -362,7 +357,7 @@ void radix_sort_pairs(bh_ctx* c, uint64_t* keys_in, uint32_t* vals_in, uint64_t*
   cudaMemsetAsync(c->sort.hist, 0, sizeof(uint32_t) * kPasses * kRadix, st);
   cudaMemsetAsync(c->sort.lookback, 0, sizeof(uint32_t) * (size_t)kPasses * tiles * kRadix, st);
   cudaMemsetAsync(c->sort.tile_ctr, 0, sizeof(uint32_t) * kPasses, st);
-  int hblocks = (int)min((long long)152 * 4, ((long long)n + kThreads * 8 - 1) / (kThreads * 8));
+  int hblocks = (int)min((long long)c->sms * 4, ((long long)n + kThreads * 8 - 1) / (kThreads * 8));
   c->launches += 2 + npasses;
   k_hist<<<hblocks, kThreads, 0, st>>>(keys_in, n, c->sort.hist);
   k_hist_scan<<<kPasses, kRadix, 0, st>>>(c->sort.hist);
@@ -425,6 +420,7 @@ constexpr int kMaxDevices = 64;
 std::mutex g_static_mutex;
 unsigned char* g_static_addr[kMaxDevices] = {};
 bool g_static_attr[kMaxDevices] = {};
+int g_static_sms[kMaxDevices] = {};
 
 }  // namespace
 }  // namespace bh
@@ -440,6 +436,7 @@ extern "C" bh_status bh_sort_keys_static(const uint64_t* keys_in, const uint32_t
     return BH_ERR_DEVICE;
   }
   unsigned char* base = nullptr;
+  int sms = 0;
   {
     std::lock_guard<std::mutex> lock(g_static_mutex);
     if (!g_static_addr[dev]) {
@@ -458,7 +455,16 @@ extern "C" bh_status bh_sort_keys_static(const uint64_t* keys_in, const uint32_t
       }
       g_static_attr[dev] = true;
     }
+    if (!g_static_sms[dev]) {
+      if (cudaDeviceGetAttribute(&g_static_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+          g_static_sms[dev] <= 0) {
+        g_static_sms[dev] = 0;
+        cudaGetLastError();
+        return BH_ERR_DEVICE;
+      }
+    }
     base = g_static_addr[dev];
+    sms = g_static_sms[dev];
   }
   cudaStream_t st = (cudaStream_t)stream;
   const int nn = (int)n;
@@ -479,7 +485,7 @@ extern "C" bh_status bh_sort_keys_static(const uint64_t* keys_in, const uint32_t
   // everything that must start at zero: histograms, look-back words, tile counters, error word
   cudaMemsetAsync(hist, 0, kOffErr + sizeof(uint32_t) - kOffHist, st);
   if (status_out) cudaMemsetAsync(status_out, 0, sizeof(uint32_t), st);
-  const int hblocks = (int)min((long long)152 * 4, ((long long)nn + kThreads * 8 - 1) / (kThreads * 8));
+  const int hblocks = (int)min((long long)sms * 4, ((long long)nn + kThreads * 8 - 1) / (kThreads * 8));
   k_hist<<<hblocks, kThreads, 0, st>>>(keys_in, nn, hist);
   k_hist_scan<<<kPasses, kRadix, 0, st>>>(hist);
   // pass p reads from (p == 0 ? input : buffer of pass p - 1) and writes the tmp buffers on

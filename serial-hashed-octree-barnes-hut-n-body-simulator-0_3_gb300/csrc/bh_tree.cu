@@ -1422,7 +1422,7 @@ void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
     k_nodes_write<<<ntiles, kPBThreads, 0, c->stream>>>(c->tkey, n, leaf_cap, span, tile, ntiles, totals, c->nkey,
                                                         c->nrange, c->wnode, c->nchildbyte, c->nparent,
                                                         c->level_bounds, (long long)c->node_cap, c->err);
-    const int lgrid = (int)std::min<size_t>(152 * 8, (c->node_cap + kThreads - 1) / kThreads);
+    const int lgrid = (int)std::min<size_t>((size_t)c->sms * 8, (c->node_cap + kThreads - 1) / kThreads);
     k_nodes_link<<<lgrid, kThreads, 0, c->stream>>>(c->level_bounds, c->nkey, c->nparent, c->nrange, c->wnode,
                                                     c->nchildbyte, c->err);
     return;
@@ -1435,7 +1435,7 @@ void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
     k_tree_init<<<1, 64, 0, c->stream>>>(n, c->nkey, c->nrange, c->level_bounds, c->level_tile_ctr);
   const int max_tiles = c->lb_level_tiles;
   cudaMemsetAsync(c->lb_level, 0, sizeof(uint32_t) * (size_t)kLevels * max_tiles, c->stream);
-  const int grid = 152 * 4;
+  const int grid = c->sms * 4;
   for (int d = 0; d < kLevels; ++d)
     k_level<<<grid, kThreads, 0, c->stream>>>(d, c->tkey, leaf_cap, c->nkey, c->nrange, c->wnode, c->nchildbyte,
                                               c->level_bounds, c->level_tile_ctr,
@@ -1446,10 +1446,10 @@ void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode, bool batch) {
   (void)leaf_cap;
   if (n <= 0) return;
   // a thread for every two bodies, about one per node or more at leaf capacity >= 2 (the climbs
-  // want a thread per leaf: at N = 2^22 a fixed 152 x 8 blocks took 0.39 ms, this 0.27 ms, the
-  // level-by-level pass it replaces 0.29 ms; at N = 2^25 a fixed 152 x 32 blocks took 2.65 ms,
+  // want a thread per leaf: at N = 2^22 a fixed 8 blocks per SM took 0.39 ms, this 0.27 ms, the
+  // level-by-level pass it replaces 0.29 ms; at N = 2^25 a fixed 32 blocks per SM took 2.65 ms,
   // this 1.54 ms)
-  const int grid = std::max(152 * 8, (n / 2 + kThreads - 1) / kThreads);
+  const int grid = std::max(c->sms * 8, (n / 2 + kThreads - 1) / kThreads);
   c->launches += 2;
   k_upsweep_links<<<grid, kThreads, 0, c->stream>>>(c->level_bounds, c->wnode, c->nparent, c->narrived, c->err);
   k_upsweep<<<grid, kThreads, 0, c->stream>>>(mode, c->level_bounds, c->nkey, c->nparent, c->narrived, c->tpos,
@@ -1478,7 +1478,7 @@ void launch_sys_keys(bh_ctx* c, const uint32_t* vals, int n, uint64_t* k2) {
 void launch_hash(bh_ctx* c) {
   cudaMemsetAsync(c->hash_keys, 0, sizeof(uint64_t) * c->hash_cap, c->stream);
   c->launches += 1;
-  k_hash_insert<<<152 * 8, kThreads, 0, c->stream>>>(c->nkey, c->level_bounds, (unsigned long long*)c->hash_keys,
+  k_hash_insert<<<c->sms * 8, kThreads, 0, c->stream>>>(c->nkey, c->level_bounds, (unsigned long long*)c->hash_keys,
                                                      c->hash_vals, c->hash_cap, (long long)c->node_cap, c->err);
 }
 
