@@ -6,7 +6,7 @@
                                 compiled unmodified from the reference checkout (read in place,
                                 never copied) against oracle/ref_shim/ofMain.h, plus the C-ABI
                                 harness oracle/ref_harness.cpp. Built only where the reference
-                                checkout exists (REFERENCE_SRC, default /root/reference/src).
+                                checkout exists (REFERENCE_ROOT, the checkout's root).
 
 Both use g++ -O2 -ffp-contract=off without -march flags, so no FMA contraction changes the
 FP64 results.
@@ -15,7 +15,17 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("REFERENCE_SRC", "/root/reference/src")
+# the reference checkout (read in place; this recipe and reference_path() are the only places
+# that name it): REFERENCE_ROOT overrides the container's mount point
+REFERENCE_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REF_SRC = os.environ.get("REFERENCE_SRC", os.path.join(REFERENCE_ROOT, "src"))
+
+
+def reference_path(*parts):
+    """A path inside the reference checkout, or None where the checkout is absent (the GPU
+    host, any other machine)."""
+    p = os.path.join(REFERENCE_ROOT, *parts)
+    return p if os.path.exists(p) else None
 REF_TUS = ["MathUtils.cpp", "Body.cpp", "OctantUtils.cpp", "HashedNode.cpp", "HashedOctree.cpp"]
 FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread"]
 

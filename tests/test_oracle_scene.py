@@ -18,7 +18,9 @@ from oracle import oracle as oracle_mod
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURE = os.path.join(HERE, "golden", "horizons_synthetic.txt")
-REF_HORIZONS = "/root/reference/horizon_results"
+from oracle.build_oracle import reference_path  # noqa: E402
+
+REF_HORIZONS = reference_path("horizon_results")  # None without the reference checkout
 
 
 @pytest.fixture(scope="module")
@@ -115,7 +117,7 @@ def test_parse_horizons_reads_values(bh):
     assert (lit[:, 1:4] == 0).mean() > 0.9 and (got[:, 1:4] != 0).all()
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_HORIZONS), reason="reference checkout not available")
+@pytest.mark.skipif(REF_HORIZONS is None, reason="reference checkout not available")
 def test_parse_horizons_reference_files(bh, ref_scene):
     files = sorted(f for f in os.listdir(REF_HORIZONS) if f.startswith("horizons_results_") and f.endswith(".txt"))
     assert files
