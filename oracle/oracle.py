@@ -234,7 +234,7 @@ class RefLiteral:
         lib.ref_sort_bodies.argtypes = [P, S, P]
         lib.ref_guard.argtypes = [P, S, P, D]
         lib.ref_guard.restype = L
-        lib.ref_build_nodes.argtypes = [P, P, S, P, D, S, P, P, P, P, P, P]
+        lib.ref_build_nodes.argtypes = [P, P, S, P, D, S, P, P, P, P, P, P, P]
         lib.ref_build_nodes.restype = L
         lib.ref_force.argtypes = [P, P, S, P, D, D, P, P]
         lib.ref_app_steps.argtypes = [P, P, P, S, D, D, D, I, P, P, P]
@@ -283,12 +283,13 @@ class RefLiteral:
         com = np.zeros((cap, 3))
         cb = np.zeros(cap, np.uint8)
         q = np.zeros((cap, 6))
+        box = np.zeros((cap, 4))
         got = self.lib.ref_build_nodes(_p(pos), _p(mass), n, _p(c), edge, cap, _p(keys), _p(counts), _p(m), _p(com),
-                                       _p(cb), _p(q))
+                                       _p(cb), _p(q), _p(box))
         if got < 0:
             raise ValueError("REF-LITERAL refused the input (duplicate depth-21 cells)")
         return dict(keys=keys[:got], counts=counts[:got], mass=m[:got], com=com[:got], child_byte=cb[:got],
-                    quad=q[:got])
+                    quad=q[:got], box=box[:got])
 
     def force(self, pos, mass, center, edge, theta):
         """Accelerations with the reference's fixed softening 0.025, and list lengths."""

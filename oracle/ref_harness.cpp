@@ -113,11 +113,14 @@ long ref_guard(const double* pos3, size_t n, const double* center3, double edge)
   return dup;
 }
 
-// Builds the reference tree over the bodies in the given (insertion) order and dumps it.
+// Builds the reference tree over the bodies in the given (insertion) order and dumps it, in
+// key order. box4 (optional) receives each node's nodeBounds as (centre x, y, z, size): the
+// cube the reference's child constructor gives it (src/HashedNode.cpp:48-56) and visualizeTree
+// draws (src/HashedOctree.cpp:939-974).
 // Returns the node count, -1 if cap is too small, -2 if the guard refuses the input.
 long ref_build_nodes(const double* pos3, const double* mass, size_t n, const double* center3, double edge,
                      size_t cap, uint64_t* keys, int64_t* counts, double* masses, double* bary3,
-                     uint8_t* childbyte, double* quad6) {
+                     uint8_t* childbyte, double* quad6, double* box4) {
   if (ref_guard(pos3, n, center3, edge) != 0) return -2;
   Body* b = make_bodies(pos3, nullptr, mass, n);
   OctantBounds root(Vec3D(center3[0], center3[1], center3[2]), edge);
@@ -143,6 +146,12 @@ long ref_build_nodes(const double* pos3, const double* mass, size_t n, const dou
     bary3[3 * j + 2] = nd->baryCenter.z;
     childbyte[j] = nd->childByte;
     for (int q = 0; q < 6; ++q) quad6[6 * j + q] = nd->quadrupoleMoment[q];
+    if (box4) {
+      box4[4 * j] = nd->nodeBounds.center.x;
+      box4[4 * j + 1] = nd->nodeBounds.center.y;
+      box4[4 * j + 2] = nd->nodeBounds.center.z;
+      box4[4 * j + 3] = nd->nodeBounds.size;
+    }
   }
   tree.deleteTree();
   delete[] b;

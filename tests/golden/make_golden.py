@@ -75,6 +75,7 @@ def literal_case(ref, pm):
         rec[f"{tag}_node_mass"] = t["mass"]
         rec[f"{tag}_node_com"] = t["com"]
         rec[f"{tag}_node_child"] = t["child_byte"]
+        rec[f"{tag}_node_box"] = t["box"]  # nodeBounds: centre x, y, z and size (FP64)
         acc, ll = ref.force(sp, sm, c, edge, THETA)
         rec[f"{tag}_acc"] = acc
         rec[f"{tag}_list_len"] = ll.astype(np.int32)
@@ -98,6 +99,7 @@ def main():
     keep = {k: rec[k] for k in ("pos_m", "center", "size", "keys", "perm", "e1_node_keys", "e1_node_counts",
                                 "e1_list_len")}
     keep["e1_acc"] = rec["e1_acc"].astype(np.float32)
+    keep["e1_node_box"] = rec["e1_node_box"].astype(np.float32)  # as the library returns node boxes
     np.savez_compressed(os.path.join(HERE, "literal_config0.npz"), **keep)
 
     # three frames of ofApp::update + draw (drawing excluded), app geometry, theta = 0.5

@@ -2,7 +2,7 @@
 
 Bars:
   * bounds size, Morton keys, sort permutation, node-key set, node body counts and child
-    bytes, literal pseudo-barycentres: bit-exact;
+    bytes, literal pseudo-barycentres, node cubes (FP64 nodeBounds rounded to FP32): bit-exact;
   * accelerations against the reference walk at the same theta, softening and leaf size:
     median relative error <= 1e-5 and 99th percentile <= 1e-4 (FP32 kernel vs FP64 oracle);
   * accelerations against the FP64 direct sum at theta = 0.5: median <= 1e-3.
@@ -60,6 +60,10 @@ def test_literal_small_cases_vs_golden(bh, sim, name):
         assert np.array_equal(t["child_byte"], g(f"{tag}_node_child"))
         assert np.array_equal(t["com"], g(f"{tag}_node_com"))
         assert np.allclose(t["mass"], g(f"{tag}_node_mass"), rtol=1e-12)
+        # node cubes (visualizeTree's boxes): the reference's FP64 nodeBounds rounded to FP32
+        box, _, count = sim.tree_boxes()
+        assert np.array_equal(box, g(f"{tag}_node_box").astype(np.float32))
+        assert np.array_equal(count, g(f"{tag}_node_counts"))
         acc, st = sim.force(0.5, 0.025, stats=True)
         if len(pm) > 1:
             assert_acc_close(acc, g(f"{tag}_acc"))
@@ -82,6 +86,7 @@ def test_literal_config0_vs_golden(bh, sim):
     t = sim.tree_nodes()
     assert np.array_equal(t["keys"], d["e1_node_keys"])
     assert np.array_equal(t["counts"], d["e1_node_counts"])
+    assert np.array_equal(sim.tree_boxes()[0], d["e1_node_box"])
     acc, st = sim.force(0.5, 0.025, stats=True)
     assert_acc_close(acc, d["e1_acc"])
     assert abs(int(st.interactions_p2p) - int(d["e1_list_len"].sum())) <= 1e-4 * d["e1_list_len"].sum()

@@ -175,3 +175,39 @@ def test_decode_morton_matches_reference(orc, ref):
     # a key decodes to its cell's low corner: within one cell of the encoded position
     dec = orc.decode_morton(keys[:5000], size)
     assert np.all(np.abs(dec - pos) <= 2 * size / 2**21 * (1 + 1e-12))
+
+
+def boxes_from_keys(keys, center, edge):
+    """Each node's cube from its key alone, by the child-bounds recurrence (FP64, one rounding
+    per operation: size' = size * 0.5; c' = c + (+-0.5) * size'), vectorised over the nodes."""
+    keys = np.asarray(keys, np.uint64)
+    depth = np.array([(int(k).bit_length() - 1) // 3 for k in keys])
+    c = np.tile(np.asarray(center, np.float64), (len(keys), 1))
+    s = np.full(len(keys), float(edge))
+    for lvl in range(int(depth.max(initial=0))):
+        live = depth > lvl  # nodes below level lvl take the step to their level-(lvl + 1) ancestor
+        shift = (3 * (depth - lvl - 1)).clip(min=0).astype(np.uint64)
+        o = ((keys >> shift) & np.uint64(7)).astype(np.int64)
+        s = np.where(live, s * 0.5, s)
+        for a in range(3):
+            half = np.where((o >> (2 - a)) & 1, 0.5, -0.5)
+            c[:, a] = np.where(live, c[:, a] + half * s, c[:, a])
+    return np.column_stack([c, s]), depth
+
+
+@pytest.mark.parametrize("name", sorted({k.split("/")[0] for k in golden("literal_small.npz").files}))
+def test_node_boxes_golden_follow_child_recurrence(name):
+    """REF-LITERAL's nodeBounds (the cubes visualizeTree draws) are the child-bounds recurrence
+    applied along each node key from the root cube, bit for bit: the rule bh_tree_boxes uses."""
+    d = golden("literal_small.npz")
+    for tag, ef in (("e1", 1.0), ("e2", 2.0)):
+        if f"{name}/{tag}_refused" in d.files:
+            continue
+        box, _ = boxes_from_keys(d[f"{name}/{tag}_node_keys"], d[f"{name}/center"], d[f"{name}/size"][0] * ef)
+        assert np.array_equal(box, d[f"{name}/{tag}_node_box"]), (name, tag)
+
+
+def test_node_boxes_golden_config0_follow_child_recurrence():
+    d = golden("literal_config0.npz")
+    box, _ = boxes_from_keys(d["e1_node_keys"], d["center"], d["size"][0])
+    assert np.array_equal(box.astype(np.float32), d["e1_node_box"])
