@@ -144,3 +144,59 @@ def test_batch_at_the_system_limit(bh):
             p, v, _ = one.get_bodies()
             assert np.array_equal(bv[a:b, 3], v[:, 3])
             assert np.allclose(bp[a:b, :3], p[:, :3], rtol=0, atol=1e-6)
+
+
+def ensemble_4096_offsets(seed=1000, nsys=4096, nmin=256, nmax=65536):
+    """The batched-ensemble configuration's layout: 4096 systems, N_s = round(exp(U ln 256 +
+    ln 256)) on [256, 65 536] (about 47 M bodies), the same draw as the ensemble benchmark."""
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(0.0, 1.0, nsys)
+    sizes = np.round(np.exp(u * np.log(nmax / nmin) + np.log(nmin))).astype(np.int64)
+    return np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint32)
+
+
+def test_batch_step_at_ensemble_4096_size(bh, orc):
+    """The full 4096-system ensemble (theta 0.6, eps 0.01, leaf 8, dt 1e-3, per-system Plummer
+    spheres from the device generator). After one batched step, a seeded sample of 40 systems
+    (at least 8 above 16 384 bodies, where the plain path sorts and builds with its multi-block
+    kernels) matches each system's own bh_step; six of them, three above 16 384 bodies, also
+    match the oracle's step (same permutation, state within 1e-6, accelerations within the
+    reference-walk bars)."""
+    off = ensemble_4096_offsets()
+    sizes = np.diff(off).astype(np.int64)
+    n = int(off[-1])
+    prm = bh.default_params(theta=0.6, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1, edge_factor=2.0)
+    rng = np.random.default_rng(11)
+    big = np.flatnonzero(sizes > 16384)
+    small = np.flatnonzero(sizes <= 16384)
+    pick = np.sort(np.concatenate([rng.choice(big, 10, replace=False), rng.choice(small, 30, replace=False)]))
+    with bh.Simulation(n) as sim:
+        sim.batch_plummer_device(1000, off)
+        pm, vel, _ = sim.get_bodies()
+        for s in range(len(sizes)):  # body id within its system rides in the unused velocity lane
+            vel[off[s]:off[s + 1], 3] = np.arange(sizes[s], dtype=np.float32)
+        sim.batch_set(pm, vel, off)
+        st = sim.batch_step(prm, 1)
+        assert st.steps == 1 and st.error_flags == 0
+        bp, bv, ba = sim.get_bodies()
+    worst = 0.0
+    with bh.Simulation(int(sizes[pick].max())) as one:
+        for s in pick:
+            a, b = int(off[s]), int(off[s + 1])
+            one.set_bodies(pm[a:b], vel[a:b])
+            one.step(prm, 1)
+            p, v, acc = one.get_bodies()
+            assert np.array_equal(bv[a:b, 3], v[:, 3]), f"system {s} ({b - a} bodies): permutation differs"
+            assert np.allclose(bp[a:b, :3], p[:, :3], rtol=0, atol=1e-6)
+            assert np.allclose(bv[a:b, :3], v[:, :3], rtol=0, atol=1e-6)
+            worst = max(worst, float(relerr(ba[a:b], acc).max()))
+    assert worst <= 1e-5
+    for s in np.concatenate([pick[np.isin(pick, big)][:3], pick[~np.isin(pick, big)][:3]]):
+        a, b = int(off[s]), int(off[s + 1])
+        out = orc.steps(pm[a:b, :3], vel[a:b, :3], pm[a:b, 3], np.zeros((b - a, 3)), 1e-3, 0.6, 0.01, 2.0, 8, 1, 1,
+                        acc_follows_body=1, nthreads=16)
+        assert np.array_equal(bv[a:b, 3].astype(np.int64), out["perm"].astype(np.int64)), s
+        assert np.allclose(bp[a:b, :3], out["pos"], rtol=0, atol=1e-6)
+        assert np.allclose(bv[a:b, :3], out["vel"], rtol=0, atol=1e-6)
+        err = relerr(ba[a:b], out["acc"])
+        assert np.median(err) <= 1e-5 and np.percentile(err, 99) <= 1e-4, (s, np.median(err), np.percentile(err, 99))
