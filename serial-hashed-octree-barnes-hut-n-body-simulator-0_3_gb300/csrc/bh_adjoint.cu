@@ -464,9 +464,7 @@ bh_status vjp(bh_ctx* c, AdjState* a, const TapeSlot& t) {
   }
   cudaMemsetAsync(a->nadj, 0, sizeof(float) * kNadj * (size_t)t.m, c->stream);
   cudaMemsetAsync(a->next, 0, sizeof(unsigned), c->stream);
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = c->sms;
   if (!a->vjp_attr) {
     BH_TRY(cuda_status(cudaFuncSetAttribute(k_vjp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVjpSmem)));
     int per_sm = 0;

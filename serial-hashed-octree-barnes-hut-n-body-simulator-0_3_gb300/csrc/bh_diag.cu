@@ -156,9 +156,7 @@ bh_status bh_energy_diag(bh_ctx* c, double theta, double eps, bh_energy* out, fl
   k_potential<<<(n + kThreads - 1) / kThreads, kThreads, 0, c->stream>>>(
       c->wnode, c->tpos, c->tslot, n, (float)(theta * theta), (float)(eps * eps),
       c->tree_mode == BH_MULTIPOLE_QUADRUPOLE ? 1 : 0, pot, sums, c->err);
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = c->sms;
   const int grid = (n + kThreads - 1) / kThreads < sms * 8 ? (n + kThreads - 1) / kThreads : sms * 8;
   k_moments<<<grid, kThreads, 0, c->stream>>>(c->pos[c->cur], c->vel[c->cur], n, sums);
   double h[kSums];

@@ -548,18 +548,24 @@ __global__ __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) void k_walk(const W
   }
 }
 
-// Persistent grid of one walk instantiation: every block that can be resident at once.
+// Persistent grid of one walk instantiation on the current device: every block that can be
+// resident at once (kept per device; bh_create fills it through walk_init before any capture).
+constexpr int kWalkMaxDevices = 64;
 template <bool kQuad, bool kSelf, bool kRec, class Cfg>
 int walk_grid() {
-  static int blocks = 0;
-  if (blocks == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
+  static int blocks[kWalkMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kWalkMaxDevices) {
+    cudaGetLastError();
+    dev = 0;
+  }
+  if (blocks[dev] == 0) {
+    int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<kQuad, kSelf, kRec, Cfg>, Cfg::kThreads, 0);
-    blocks = max(1, sms * max(1, per_sm));
+    blocks[dev] = max(1, sms * max(1, per_sm));
   }
-  return blocks;
+  return blocks[dev];
 }
 
 template <bool kQuad, bool kSelf, class Cfg = CfgDefault>
