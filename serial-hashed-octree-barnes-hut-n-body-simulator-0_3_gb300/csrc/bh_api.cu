@@ -637,20 +637,24 @@ bool pinned(const void* p) {
 
 // One plain step enqueued on c->stream without host synchronisation (capturable). Stage events
 // are external event-record nodes when captured (a plain record during capture would only order
-// the capture, not record the event). With io, the copies run on c->copy_stream beside the step:
-// the velocities upload while bounds, keys and sort run; the positions, final after the drift,
-// download while the tree is built and walked; the velocities download after the walk's kick.
+// the capture, not record the event). With io, the positions upload first, then the copies run
+// on c->copy_stream beside the step: the velocities upload while bounds, keys and sort run; the
+// positions, final after the drift, download while the tree is built and walked; the velocities
+// download after the walk's kick.
 void enqueue_plain_step(bh_ctx* c, const bh_params* prm, const HostIO* io) {
   const int n = (int)c->n, cur = c->cur, nx = 1 - cur;
   const float dt = (float)prm->dt;
   const size_t bytes = sizeof(float4) * (size_t)n;
   auto mark = [&](int k) { cudaEventRecordWithFlags(c->stage_ev[k], c->stream, cudaEventRecordExternal); };
   if (io) {
+    // positions first, alone on the link (the bounds wait for them); the velocities follow on
+    // the second stream beside bounds, keys and sort (two uploads at once would share the
+    // link's bandwidth and delay the positions)
+    if (io->pos_in) cudaMemcpyAsync(c->pos[cur], io->pos_in, bytes, cudaMemcpyHostToDevice, c->stream);
     cudaEventRecord(c->io_ev[0], c->stream);  // fork
     cudaStreamWaitEvent(c->copy_stream, c->io_ev[0], 0);
     if (io->vel_in) cudaMemcpyAsync(c->vel[cur], io->vel_in, bytes, cudaMemcpyHostToDevice, c->copy_stream);
     cudaEventRecord(c->io_ev[1], c->copy_stream);
-    if (io->pos_in) cudaMemcpyAsync(c->pos[cur], io->pos_in, bytes, cudaMemcpyHostToDevice, c->stream);
   }
   clear_device_flags(c);
   mark(0);
@@ -940,11 +944,11 @@ void enqueue_batch_step(bh_ctx* c, const bh_params& p, const HostIO* io) {
   const float dt = (float)p.dt;
   const size_t bytes = sizeof(float4) * (size_t)n;
   if (io) {  // the copies of bh_batch_step_host, beside the step as in enqueue_plain_step
+    if (io->pos_in) cudaMemcpyAsync(c->pos[cur], io->pos_in, bytes, cudaMemcpyHostToDevice, c->stream);
     cudaEventRecord(c->io_ev[0], c->stream);
     cudaStreamWaitEvent(c->copy_stream, c->io_ev[0], 0);
     if (io->vel_in) cudaMemcpyAsync(c->vel[cur], io->vel_in, bytes, cudaMemcpyHostToDevice, c->copy_stream);
     cudaEventRecord(c->io_ev[1], c->copy_stream);
-    if (io->pos_in) cudaMemcpyAsync(c->pos[cur], io->pos_in, bytes, cudaMemcpyHostToDevice, c->stream);
   }
   // stage events as in the plain step (external event-record nodes in the captured graph)
   auto mark = [&](int k) { cudaEventRecordWithFlags(c->stage_ev[k], c->stream, cudaEventRecordExternal); };
