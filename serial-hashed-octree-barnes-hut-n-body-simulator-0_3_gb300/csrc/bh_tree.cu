@@ -981,6 +981,10 @@ __device__ __forceinline__ NodeUp load_nodeup(const NodeUp* p) {
 // The multipole of one node at depth d (computeTreeBaryCenters / computeNodeBaryCenters,
 // src/HashedOctree.cpp:721-855, as intended; or the literal pseudo-barycentres). A leaf
 // combines its member bodies, an internal node its children, whose records are complete.
+// kPrefetch (small trees, where the climb's latency is the upsweep's time): an internal node
+// loads all its children's records at once before combining them, one L2 round trip instead of
+// one per child and pass; the arithmetic and its order are the same, so are the results.
+template <bool kPrefetch>
 __device__ void upsweep_node(int node, int d, int mode, const float4* __restrict__ tpos,
                              const uint32_t* __restrict__ tslot, WalkNode* __restrict__ wn, NodeUp* __restrict__ nf,
                              const Geom* __restrict__ g, const uint16_t* __restrict__ body_sys) {
@@ -1055,6 +1059,46 @@ __device__ void upsweep_node(int node, int d, int mode, const float4* __restrict
           }
         }
       }
+    } else if (kPrefetch) {
+      NodeUp ch[8];
+      int cw[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (k < link.y) {
+          ch[k] = load_nodeup(nf + link.x + k);
+          cw[k] = mode == BH_MULTIPOLE_LITERAL ? 0 : wn[link.x + k].link.w;
+        }
+      if (mode == BH_MULTIPOLE_LITERAL) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          if (k < link.y) {
+            mass = ff_add(mass, {ch[k].mass_hi, ch[k].mass_lo});
+            if (ch[k].min_rank < min_rank) {
+              min_rank = ch[k].min_rank;
+              for (int a = 0; a < 3; ++a) com[a] = {ch[k].com_hi[a], ch[k].com_lo[a]};
+            }
+          }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          if (k < link.y) {
+            const FF m = {ch[k].mass_hi, ch[k].mass_lo};
+            mass = ff_add(mass, m);
+            for (int a = 0; a < 3; ++a) com[a] = ff_add(com[a], ff_mul({ch[k].com_hi[a], ch[k].com_lo[a]}, m));
+            min_rank = min(min_rank, ch[k].min_rank);
+          }
+        if (mass.hi != 0.f)
+          for (int a = 0; a < 3; ++a) com[a] = ff_div(com[a], mass);
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          if (k < link.y) {
+            quad_add(q, ch[k].mass_hi, (ch[k].com_hi[0] - com[0].hi) + (ch[k].com_lo[0] - com[0].lo),
+                     (ch[k].com_hi[1] - com[1].hi) + (ch[k].com_lo[1] - com[1].lo),
+                     (ch[k].com_hi[2] - com[2].hi) + (ch[k].com_lo[2] - com[2].lo));
+            if (cw[k] > 1)
+              for (int j = 0; j < 6; ++j) q[j] += ch[k].q[j];
+          }
+      }
     } else {
       if (mode == BH_MULTIPOLE_LITERAL) {
         for (int c = link.x; c < link.x + link.y; ++c) {
@@ -1124,6 +1168,7 @@ __global__ __launch_bounds__(kThreads) void k_upsweep_links(const int* __restric
 // from all its children, in child order, and goes on up. Every node is computed once, from
 // complete children, with the arithmetic and order of a level-by-level pass, and no thread
 // ever waits for another.
+template <bool kPrefetch>
 __global__ __launch_bounds__(kThreads) void k_upsweep(int mode, const int* __restrict__ level_bounds,
                                                       const uint64_t* __restrict__ nkey,
                                                       const int* __restrict__ parent, uint32_t* __restrict__ arrived,
@@ -1141,14 +1186,16 @@ __global__ __launch_bounds__(kThreads) void k_upsweep(int mode, const int* __res
     int d = (63 - __clzll((long long)nkey[i])) / 3;
     deepest = max(deepest, (unsigned)d);
     for (;;) {
-      upsweep_node(node, d, mode, tpos, tslot, wn, nf, g, body_sys);
+      upsweep_node<kPrefetch>(node, d, mode, tpos, tslot, wn, nf, g, body_sys);
       const int p = parent[node];
       if (p < 0) break;
+      // the parent's child count (written by the build) can be read before the arrival atomic
+      const int pchildren = kPrefetch ? wn[p].link.y : 0;
       // acquire-release: this node's stores are visible to the thread that completes the
       // parent, and that thread sees every child's stores
       unsigned prev;
       asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(arrived + p) : "memory");
-      if (prev + 1u < (unsigned)wn[p].link.y) break;
+      if (prev + 1u < (unsigned)(kPrefetch ? pchildren : wn[p].link.y)) break;
       node = p;
       --d;
     }
@@ -1442,6 +1489,12 @@ void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
                                               c->lb_level + (size_t)d * max_tiles, (long long)c->node_cap, c->err);
 }
 
+#ifndef BH_UPSWEEP_PREFETCH_MAX
+#define BH_UPSWEEP_PREFETCH_MAX 65536
+#endif
+// systems of at most this many bodies climb with the children's records prefetched
+constexpr int kUpsweepPrefetchMaxBodies = BH_UPSWEEP_PREFETCH_MAX;
+
 void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode, bool batch) {
   (void)leaf_cap;
   if (n <= 0) return;
@@ -1452,7 +1505,12 @@ void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode, bool batch) {
   const int grid = std::max(c->sms * 8, (n / 2 + kThreads - 1) / kThreads);
   c->launches += 2;
   k_upsweep_links<<<grid, kThreads, 0, c->stream>>>(c->level_bounds, c->wnode, c->nparent, c->narrived, c->err);
-  k_upsweep<<<grid, kThreads, 0, c->stream>>>(mode, c->level_bounds, c->nkey, c->nparent, c->narrived, c->tpos,
+  // the prefetching climb holds eight children's records in registers (one block per SM): two
+  // threads per body there (about one per node at leaf capacity 1), at least a block per SM
+  const bool prefetch = n <= kUpsweepPrefetchMaxBodies;
+  auto upsweep = prefetch ? k_upsweep<true> : k_upsweep<false>;
+  const int ugrid = prefetch ? std::max(c->sms, (2 * n + kThreads - 1) / kThreads) : grid;
+  upsweep<<<ugrid, kThreads, 0, c->stream>>>(mode, c->level_bounds, c->nkey, c->nparent, c->narrived, c->tpos,
                                               c->tslot, c->wnode, c->nup, batch ? c->sys_geom : c->geom,
                                               batch ? c->body_sys : nullptr, c->err, c->counters);
 }
