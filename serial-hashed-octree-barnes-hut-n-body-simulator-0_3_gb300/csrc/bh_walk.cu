@@ -590,7 +590,10 @@ using Cfg6 = WalkCfg<8, 4, 384, 1>;
 using Cfg7 = WalkCfg<4, 8, 384, 1>;
 // variants 8 and 9: the default shape with groups of 16 and 8 bodies (single systems; more,
 // smaller groups fill the GPU when N is small)
-constexpr int kVariants = 10;
+// variants 10 and 11: 104 registers (two 8-warp blocks per SM) with groups of 16 and 8 bodies:
+// small single systems, where a few warps per SM walk and the walk's time is one warp's chain of
+// dependent latencies, which more registers let the compiler overlap
+constexpr int kVariants = 12;
 
 template <class Cfg>
 WalkVariant variant_info(int group = 32) {
@@ -611,6 +614,8 @@ void launch_quad_variant(bh_ctx* c, int v, int n, float theta2, float eps2, floa
     case 7: launch_walk_t<true, false, Cfg7>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
     case 8: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, 16); break;
     case 9: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, 8); break;
+    case 10: launch_walk_t<true, false, Cfg2>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, 16); break;
+    case 11: launch_walk_t<true, false, Cfg2>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, 8); break;
     default: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
   }
 }
@@ -630,6 +635,8 @@ WalkVariant walk_variant_info(int v) {
     case 7: return variant_info<Cfg7>();
     case 8: return variant_info<CfgDefault>(16);
     case 9: return variant_info<CfgDefault>(8);
+    case 10: return variant_info<Cfg2>(16);
+    case 11: return variant_info<Cfg2>(8);
     default: return variant_info<CfgDefault>();
   }
 }

@@ -55,7 +55,7 @@ def test_autotune_batched_then_step(bh):
     assert float(np.median(relerr(out[0][2], out[1][2]))) < 1e-5
 
 
-@pytest.mark.parametrize("variant", range(10))
+@pytest.mark.parametrize("variant", range(12))
 def test_every_walk_variant_matches_oracle(bh, orc, variant):
     """Each launch shape (cell-evaluation form, group size) the tuner can pick gives the reference's
     interaction sets and accelerations within the parity bars. The body count leaves the last
