@@ -641,11 +641,13 @@ bool pinned(const void* p) {
 // on c->copy_stream beside the step: the velocities upload while bounds, keys and sort run; the
 // positions, final after the drift, download while the tree is built and walked; the velocities
 // download after the walk's kick.
-void enqueue_plain_step(bh_ctx* c, const bh_params* prm, const HostIO* io) {
+void enqueue_plain_step(bh_ctx* c, const bh_params* prm, const HostIO* io, bool marks) {
   const int n = (int)c->n, cur = c->cur, nx = 1 - cur;
   const float dt = (float)prm->dt;
   const size_t bytes = sizeof(float4) * (size_t)n;
-  auto mark = [&](int k) { cudaEventRecordWithFlags(c->stage_ev[k], c->stream, cudaEventRecordExternal); };
+  auto mark = [&](int k) {
+    if (marks) cudaEventRecordWithFlags(c->stage_ev[k], c->stream, cudaEventRecordExternal);
+  };
   if (io) {
     // positions first, alone on the link (the bounds wait for them); the velocities follow on
     // the second stream beside bounds, keys and sort (two uploads at once would share the
@@ -699,6 +701,7 @@ bool same_io(const HostIO& a, const void* const b[4]) {
 // carry the host copies, captured per set of host buffers.
 bh_status run_plain_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats* st, const HostIO* io) {
   BH_TRY(ensure_nodes(c, initial_node_cap(c->n)));
+  const bool marks = st != nullptr;  // stage events only for calls that return their times
   const uint64_t launches0 = c->launches;
   if (!same_params(c->graph_params, *prm)) destroy_graphs(c);
   c->graph_params = *prm;
@@ -709,8 +712,10 @@ bh_status run_plain_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats*
       cudaGraphExec_t& graph = io ? c->host_graph[par] : c->graph[par];
       uint64_t*& keys0 = io ? c->host_graph_keys0[par] : c->graph_keys0[par];
       uint64_t& kernels = io ? c->host_graph_kernels[par] : c->graph_kernels[par];
-      // captured with other key buffers (they swap every step) or other host buffers
-      if (graph && (keys0 != c->keys[0] || (io && !same_io(*io, c->host_graph_ptrs[par])))) {
+      bool& gmarks = io ? c->host_graph_marks[par] : c->graph_marks[par];
+      // captured with other key buffers (they swap every step), other host buffers, or with
+      // stage events when these are (not) wanted now
+      if (graph && (keys0 != c->keys[0] || gmarks != marks || (io && !same_io(*io, c->host_graph_ptrs[par])))) {
         cudaGraphExecDestroy(graph);
         graph = nullptr;
       }
@@ -719,7 +724,8 @@ bh_status run_plain_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats*
         cudaGraph_t g = nullptr;
         BH_TRY(cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)));
         const uint64_t l0 = c->launches;
-        enqueue_plain_step(c, prm, io);
+        enqueue_plain_step(c, prm, io, marks);
+        gmarks = marks;
         kernels = c->launches - l0;  // counted when the graph runs, not when captured
         c->launches = l0;
         cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
@@ -939,7 +945,7 @@ bool same_params(const bh_params& a, const bh_params& b) {
 }
 
 // One batched step, enqueued on c->stream without host synchronisation (capturable).
-void enqueue_batch_step(bh_ctx* c, const bh_params& p, const HostIO* io) {
+void enqueue_batch_step(bh_ctx* c, const bh_params& p, const HostIO* io, bool marks) {
   const int n = (int)c->n, cur = c->cur, nx = 1 - cur;
   const float dt = (float)p.dt;
   const size_t bytes = sizeof(float4) * (size_t)n;
@@ -951,7 +957,9 @@ void enqueue_batch_step(bh_ctx* c, const bh_params& p, const HostIO* io) {
     cudaEventRecord(c->io_ev[1], c->copy_stream);
   }
   // stage events as in the plain step (external event-record nodes in the captured graph)
-  auto mark = [&](int k) { cudaEventRecordWithFlags(c->stage_ev[k], c->stream, cudaEventRecordExternal); };
+  auto mark = [&](int k) {
+    if (marks) cudaEventRecordWithFlags(c->stage_ev[k], c->stream, cudaEventRecordExternal);
+  };
   clear_device_flags(c);
   mark(0);
   bh::launch_batch_bounds(c, c->pos[c->cur], p.edge_factor);
@@ -1092,6 +1100,7 @@ bh_status run_batch_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats*
   BH_TRY(ensure_nodes(c, need));
   if (!same_params(c->graph_params, *prm)) destroy_graphs(c);
   c->graph_params = *prm;
+  const bool marks = st != nullptr;  // stage events only for calls that return their times
   const uint64_t launches0 = c->launches;
   for (int s = 0; s < nsteps; ++s) {
     uint32_t e = 0;
@@ -1100,8 +1109,10 @@ bh_status run_batch_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats*
       cudaGraphExec_t& graph = io ? c->host_graph[par] : c->graph[par];
       uint64_t*& keys0 = io ? c->host_graph_keys0[par] : c->graph_keys0[par];
       uint64_t& kernels = io ? c->host_graph_kernels[par] : c->graph_kernels[par];
-      // a plain step's graph (it records its key buffer), or other host buffers
-      if (graph && (keys0 || (io && !same_io(*io, c->host_graph_ptrs[par])))) {
+      bool& gmarks = io ? c->host_graph_marks[par] : c->graph_marks[par];
+      // a plain step's graph (it records its key buffer), other host buffers, or stage events
+      // when these are (not) wanted now
+      if (graph && (keys0 || gmarks != marks || (io && !same_io(*io, c->host_graph_ptrs[par])))) {
         cudaGraphExecDestroy(graph);
         graph = nullptr;
       }
@@ -1111,7 +1122,8 @@ bh_status run_batch_steps(bh_ctx* c, const bh_params* prm, int nsteps, bh_stats*
         BH_TRY(cuda_status(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal)));
         keys0 = nullptr;
         const uint64_t l0 = c->launches;
-        enqueue_batch_step(c, *prm, io);
+        enqueue_batch_step(c, *prm, io, marks);
+        gmarks = marks;
         kernels = c->launches - l0;  // counted when the graph runs, not when captured
         c->launches = l0;
         cudaError_t ce = cudaStreamEndCapture(c->stream, &g);

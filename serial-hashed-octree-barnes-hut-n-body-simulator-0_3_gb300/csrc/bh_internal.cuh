@@ -186,6 +186,10 @@ struct bh_ctx {
   bh_params graph_params = {};
   uint64_t graph_kernels[2] = {0, 0};  // kernel launches inside each captured graph
   uint64_t* graph_keys0[2] = {nullptr, nullptr};  // plain step graphs: the key buffer they were captured with
+  // whether each graph records the per-stage events (captured so only for calls that return
+  // stats: each event-record node costs about 4.6 us of graph time)
+  bool graph_marks[2] = {false, false};
+  bool host_graph_marks[2] = {false, false};
   size_t graph_n = 0;                              // plain step graphs: the body count they were captured for
   // bh_step_host: the step with its host copies on a second stream, one graph per state parity
   cudaStream_t copy_stream = nullptr;
