@@ -675,7 +675,7 @@ def measure_ensemble(bh, dist, steps, warmup, loop_sample, with_cpu):
             "timing": "per-step CUDA events inside the captured step; L2 flushed between steps",
             "e2e": {"value": n / (statistics.median(e2e) * 1e-3), "unit": "body-steps/s",
                     "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
-                    "ms_per_step": statistics.median(e2e)},
+                    "ms_per_step": statistics.median(e2e), "samples_ms": e2e},
             "plain_loop": {"value": n / loop_step_s, "unit": "body-steps/s", "seconds_per_step": loop_step_s,
                            "sample": (f"all {e['nsys']} systems" if len(sample) == e["nsys"] else
                                       f"{len(sample)} seeded systems, sum scaled by {e['nsys']}/{len(sample)}") +
