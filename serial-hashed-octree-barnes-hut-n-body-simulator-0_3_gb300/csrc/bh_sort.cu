@@ -24,7 +24,7 @@ constexpr int kWarps = kThreads / 32;
 #define BH_SORT_ITEMS 16
 #endif
 #ifndef BH_SORT_MIN_BLOCKS
-#define BH_SORT_MIN_BLOCKS 2
+#define BH_SORT_MIN_BLOCKS 3
 #endif
 constexpr int kItems = BH_SORT_ITEMS;     // keys per thread
 constexpr int kTile = kThreads * kItems;  // 4096 keys
@@ -35,6 +35,7 @@ constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValMask = (1u << 30) - 1;
 constexpr int kSpinLimit = 1 << 22;  // about a second of polling; then the sort reports a timeout
 constexpr int kLookWindow = 8;       // predecessor tiles read per look-back round trip
+
 
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
   uint32_t v;
@@ -115,7 +116,7 @@ struct OnesweepSmem {
   uint32_t tile;
 };
 
-// Two resident blocks per SM (the shared-memory tile allows three; registers cap it at two).
+// Three resident blocks per SM (80 registers; the shared-memory tile allows three).
 __global__ __launch_bounds__(kThreads, BH_SORT_MIN_BLOCKS) void k_onesweep(const uint64_t* __restrict__ kin,
                                                        const uint32_t* __restrict__ vin,
                                                        uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
@@ -133,8 +134,10 @@ __global__ __launch_bounds__(kThreads, BH_SORT_MIN_BLOCKS) void k_onesweep(const
   const long long base = (long long)tile * kTile;
   const int valid_count = (int)min((long long)kTile, (long long)n - base);
 
+  // the keys only: the values are read when the tile is staged, after the ranking, which keeps
+  // the ranking at 80 registers and three blocks per SM (two at 128 with the values held from
+  // the start: 0.669 -> 0.623 ms per sort at 2^23 keys, 4.62 -> 4.09 ms at 4.7e7)
   uint64_t key[kItems];
-  uint32_t val[kItems];
   uint32_t rank[kItems];
   const long long wbase = base + (long long)w * (32 * kItems);
 #pragma unroll
@@ -142,7 +145,6 @@ __global__ __launch_bounds__(kThreads, BH_SORT_MIN_BLOCKS) void k_onesweep(const
     long long idx = wbase + j * 32 + lane;
     bool ok = idx < n;
     key[j] = ok ? kin[idx] : 0ull;
-    val[j] = ok ? vin[idx] : 0u;
   }
   const uint32_t lt_mask = (1u << lane) - 1u;
 #pragma unroll
@@ -201,7 +203,7 @@ __global__ __launch_bounds__(kThreads, BH_SORT_MIN_BLOCKS) void k_onesweep(const
       uint32_t d = (uint32_t)(key[j] >> shift) & 0xFFu;
       uint32_t lp = s.digit_start[d] + s.warp_cnt[w][d] + rank[j];
       s.keys[lp] = key[j];
-      s.vals[lp] = val[j];
+      s.vals[lp] = vin[idx];
     }
   }
 

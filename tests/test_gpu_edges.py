@@ -224,3 +224,33 @@ def test_caller_stream(bh):
     finally:
         for x in bufs:
             x.free()
+
+
+@pytest.mark.parametrize("n", [4444, 70000])
+def test_stats_and_no_stats_steps_identical(bh, n):
+    """Step graphs record their stage events only for calls that return stats; a context switching
+    between the two kinds of call (re-capturing its graphs each time) follows the same trajectory
+    bit for bit as one that never asks for stats, for the plain step and the ensemble step."""
+    pm, vel = bh.plummer(13, n)
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1, edge_factor=2.0)
+    pattern = (True, False, False, True, True, False, True)
+    with bh.Simulation(n) as a, bh.Simulation(n) as b:
+        a.set_bodies(pm, vel)
+        b.set_bodies(pm, vel)
+        for want in pattern:
+            st = a.step(prm, 1, stats=want)
+            b.step(prm, 1, stats=False)
+            if want:
+                assert st.steps == 1 and st.ms_step > 0 and st.ms_walk > 0
+        for x, y in zip(a.get_bodies(), b.get_bodies()):
+            assert np.array_equal(x, y)
+        off = np.array([0, n // 3, n], np.uint32)
+        a.batch_set(pm, vel, off)
+        b.batch_set(pm, vel, off)
+        for want in pattern[:4]:
+            st = a.batch_step(prm, 1, stats=want)
+            b.batch_step(prm, 1, stats=False)
+            if want:
+                assert st.steps == 1 and st.ms_step > 0
+        for x, y in zip(a.get_bodies(), b.get_bodies()):
+            assert np.array_equal(x, y)
