@@ -628,7 +628,9 @@ def measure_ensemble(bh, dist, steps, warmup, loop_sample, with_cpu):
     pv.array[:] = cur_v
     sim.batch_step_host(prm, pp.array, pv.array, op.array, ov.array, stats=False)
     e2e = []
-    for _ in range(3):
+    # seven calls, the median reported: some runs showed one or two calls of 150-230 ms among
+    # ~118 ms ones (the 1.5 GB host copies), and three calls let two such outliers set the median
+    for _ in range(7):
         sim.event_record(0)
         sim.batch_step_host(prm, pp.array, pv.array, op.array, ov.array, stats=False)
         sim.event_record(1)
