@@ -340,8 +340,10 @@ def test_reference_body_layout_roundtrip(bh, sim):
 
 
 def test_full_size_keys_perm_nodes(bh, orc):
-    """N = 2^22 (the at-scale Plummer size): keys, permutation and node set bit-exact; forces on
-    a seeded subsample against the oracle and the FP64 direct sum."""
+    """N = 2^22 (the at-scale Plummer size): keys, permutation and node set bit-exact; step-0
+    forces against the reference's tree walk (the oracle, same theta, softening and leaf size) on
+    a seeded 65 536-body subsample at theta 0.5 and 8192 bodies at theta 0.3 and 0.7, and against
+    the FP64 direct sum."""
     n = 1 << 22
     pm, v = bh.plummer(0, n)
     pos = pm[:, :3].astype(np.float64)
@@ -359,12 +361,14 @@ def test_full_size_keys_perm_nodes(bh, orc):
         s.build(c, 2 * size, 16, bh.BH_MULTIPOLE_QUADRUPOLE)
         t = s.tree_nodes()
         assert np.array_equal(t["keys"], orc.build(p2, m2, c, 2 * size, 16, 1)["keys"])
-        acc = s.force(0.5, 0.005)
-        tgt = np.random.default_rng(0).choice(n, 4096, replace=False).astype(np.uint32)
-        ref_acc, _, _ = orc.force(p2, m2, c, 2 * size, 16, 1, 0.5, 0.005, targets=tgt, nthreads=16)
-        assert_acc_close(acc[tgt], ref_acc)
-        direct = orc.direct(p2, m2, 0.005, targets=tgt[:512], nthreads=16)
-        assert np.median(relerr(acc[tgt[:512]], direct)) <= 1e-3
+        for theta, ntgt in ((0.5, 65536), (0.3, 8192), (0.7, 8192)):
+            acc = s.force(theta, 0.005)
+            tgt = np.sort(np.random.default_rng(0).choice(n, ntgt, replace=False)).astype(np.uint32)
+            ref_acc, _, _ = orc.force(p2, m2, c, 2 * size, 16, 1, theta, 0.005, targets=tgt, nthreads=16)
+            assert_acc_close(acc[tgt], ref_acc)
+            if theta == 0.5:
+                direct = orc.direct(p2, m2, 0.005, targets=tgt[:512], nthreads=16)
+                assert np.median(relerr(acc[tgt[:512]], direct)) <= 1e-3
 
 
 def _near_boundaries(rng, n, points):
@@ -469,3 +473,38 @@ def test_full_size_step_properties(bh):
         assert np.array_equal(again, np.arange(n, dtype=again.dtype))
         keys = s.morton_keys(size)
         assert np.all(keys[1:] >= keys[:-1])
+
+
+def test_config0_trajectory_100_steps(bh, orc):
+    """The small configuration run to its full length: N = 16 384 Plummer (seed 0), theta 0.5,
+    eps 0.01, leaf 1, dt 1e-3, 100 KDK steps through bh_step (FP32) against the oracle's 100 steps
+    (FP64, the reference's step order with intended multipoles), body by body (ids ride in the
+    velocity lane): positions and velocities stay within FP32 drift of the FP64 trajectory."""
+    n, nsteps = 16384, 100
+    pm, v = bh.plummer(0, n)
+    v[:, 3] = np.arange(n, dtype=np.float32)
+    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=1, multipole=1, edge_factor=2.0)
+    with bh.Simulation(n) as s:
+        s.set_bodies(pm, v)
+        st = s.step(prm, nsteps)
+        assert st.steps == nsteps and st.error_flags == 0
+        p, vv, _ = s.get_bodies()
+    ids = vv[:, 3].astype(np.int64)
+    assert np.array_equal(np.sort(ids), np.arange(n))
+    out = orc.steps(pm[:, :3], v[:, :3], pm[:, 3], np.zeros((n, 3)), 1e-3, 0.5, 0.01, 2.0, 1, 1, nsteps,
+                    acc_follows_body=1, nthreads=16)
+    xo = np.empty((n, 3))
+    vo = np.empty((n, 3))
+    xo[out["perm"].astype(np.int64)] = out["pos"]
+    vo[out["perm"].astype(np.int64)] = out["vel"]
+    xg = np.empty((n, 3))
+    vg = np.empty((n, 3))
+    xg[ids] = p[:, :3]
+    vg[ids] = vv[:, :3]
+    dx = np.linalg.norm(xg - xo, axis=1)
+    dv = np.linalg.norm(vg - vo, axis=1)
+    print(f"config 0, 100 steps: |dx| median {np.median(dx):.2e} max {dx.max():.2e}; "
+          f"|dv| median {np.median(dv):.2e} max {dv.max():.2e}")
+    # measured: |dx| median 1.6e-7, max 8.9e-6; |dv| median 1.7e-7, max 3.9e-6
+    assert np.median(dx) <= 1e-6 and dx.max() <= 1e-4
+    assert np.median(dv) <= 1e-6 and dv.max() <= 1e-4
