@@ -665,6 +665,13 @@ void walk_init() {
   walk_grid<true, false, false, Cfg7>();
 }
 
+#ifndef BH_LITERAL_MIN_GROUP
+#define BH_LITERAL_MIN_GROUP 4
+#endif
+// smallest group of the literal walk (the app's frame, 4 444 bodies: groups of 8 / 4 / 2 walk in
+// 55.1 / 50.5 / 50.5 us)
+constexpr int kLiteralMinGroup = BH_LITERAL_MIN_GROUP;
+
 void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc_slot, float4* vel_kick,
                  float half_dt, bool batch) {
   if (n <= 0) return;
@@ -679,11 +686,11 @@ void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc
     else
       launch_quad_variant(c, c->walk_variant, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
   } else {
-    // the literal walk has no tuned variants: its group size follows N, the largest of 32, 16
-    // and 8 bodies that still gives at least 1024 groups (about seven warps per SM; the tuned
+    // the literal walk has no tuned variants: its group size follows N, the largest of 32, 16,
+    // 8 and 4 bodies that still gives at least 1024 groups (about seven warps per SM; the tuned
     // quadrupole walk picks 8 at 4 444 bodies, 16 at 16 384 and 32 at 2^22)
     int gsize = 32;
-    while (gsize > 8 && (n + gsize - 1) / gsize < 1024) gsize /= 2;
+    while (gsize > kLiteralMinGroup && (n + gsize - 1) / gsize < 1024) gsize /= 2;
     if (self)
       launch_walk_t<false, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, gsize);
     else
