@@ -601,7 +601,7 @@ def measure_ensemble(bh, dist, steps, warmup, loop_sample, with_cpu):
     tune = sim.autotune(e["theta"], e["eps"], trials=2)  # walk launch shape for this ensemble
     for _ in range(warmup - 1):  # re-captures the step graph with the chosen walk
         sim.batch_step(prm, 1, stats=False)
-    per_step, flops, walk_ms = [], [], []
+    per_step, flops, walk_ms, util = [], [], [], []
     stage = {}
     launches = 0
     dist.barrier()
@@ -613,6 +613,7 @@ def measure_ensemble(bh, dist, steps, warmup, loop_sample, with_cpu):
             per_step.append(st.ms_step)
             walk_ms.append(st.ms_walk)
             flops.append(FLOPS_P2P * st.interactions_p2p + FLOPS_CELL_QUAD * st.interactions_cell)
+            util.append((st.interactions_cell, st.walk_cell_evals, st.interactions_p2p, st.walk_point_evals))
             for key, val in st.as_dict().items():
                 if key.startswith("ms_"):
                     stage[key] = stage.get(key, 0.0) + val
@@ -692,6 +693,10 @@ def measure_ensemble(bh, dist, steps, warmup, loop_sample, with_cpu):
                          "traffic": None, "flops_per_launch": statistics.mean(flops),
                          "ms_per_launch": statistics.mean(walk_ms)},
             "stage_ms_per_step": {k[3:]: v / steps for k, v in stage.items()},
+            "walk_lane_utilization": {
+                "cells": sum(u[0] for u in util) / max(1, 32 * sum(u[1] for u in util)),
+                "points": sum(u[2] for u in util) / max(1, 32 * sum(u[3] for u in util))},
+            "interactions_per_body": statistics.mean(u[0] + u[2] for u in util) / n,
             "clocks": clocks.summary()}
     if cpu:
         line["cpu_baseline"] = cpu
