@@ -199,9 +199,11 @@ bh_status bh_step(bh_ctx* ctx, const bh_params* params, int nsteps, bh_stats* st
  * The state keeps its accelerations, so a loop of calls is the same trajectory as bh_step.
  * Any pointer may be null (no copy). With page-locked buffers (bh_host_alloc or registered
  * memory) the copies overlap the step on a second stream: the velocity upload runs beside the
- * bounds, keys and sort, the position download beside the tree build and walk; the step and its
- * copies are one CUDA graph per state parity, re-captured when the buffers change. With pageable
- * buffers the copies run before and after the step. */
+ * bounds, keys and sort, the position download beside the tree build and walk; a page-locked
+ * velocity output that is mapped into the device's address space and 16-byte aligned is written
+ * by the walk's closing kick itself (no download after the walk), any other one is downloaded
+ * after the walk. The step and its copies are one CUDA graph per state parity, re-captured when
+ * the buffers change. With pageable buffers the copies run before and after the step. */
 bh_status bh_step_host(bh_ctx* ctx, const bh_params* params, const float* pos_m4_in, const float* vel4_in,
                        float* pos_m4_out, float* vel4_out, bh_stats* stats);
 

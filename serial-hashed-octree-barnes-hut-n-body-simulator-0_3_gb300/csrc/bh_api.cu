@@ -605,13 +605,28 @@ bh_status bh_kick(bh_ctx* c, double dt) {
 
 namespace {
 
-// Host buffers of bh_step_host (pinned; any may be null).
+// Host buffers of bh_step_host (pinned; any may be null). vel_out_dev is vel_out's address in
+// the device's address space when the buffer is mapped and 16-byte aligned: the walk's kick then
+// writes the velocities there itself and no download follows the walk.
 struct HostIO {
   const float* pos_in;
   const float* vel_in;
   float* pos_out;
   float* vel_out;
+  float4* vel_out_dev;
 };
+
+// Device address of a pinned host buffer for direct float4 stores, or null (not mapped, or not
+// 16-byte aligned).
+float4* mapped_float4(void* host) {
+  if (!host) return nullptr;
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, host, 0) != cudaSuccess || !d) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (reinterpret_cast<uintptr_t>(d) % alignof(float4)) == 0 ? static_cast<float4*>(d) : nullptr;
+}
 
 bh_status ensure_copy_stream(bh_ctx* c);  // the second stream of the *_step_host calls
 
@@ -684,10 +699,13 @@ void enqueue_plain_step(bh_ctx* c, const bh_params* prm, const HostIO* io, bool 
   mark(6);
   bh::launch_upsweep(c, n, prm->leaf_capacity, prm->multipole);
   mark(7);
-  bh::launch_walk(c, n, (float)prm->theta, (float)prm->eps, prm->multipole, c->acc, c->vel[nx], 0.5f * dt);
+  float4* vel_copy = io ? io->vel_out_dev : nullptr;
+  bh::launch_walk(c, n, (float)prm->theta, (float)prm->eps, prm->multipole, c->acc, c->vel[nx], 0.5f * dt, false,
+                  vel_copy);
   mark(8);
   if (io) {
-    if (io->vel_out) cudaMemcpyAsync(io->vel_out, c->vel[nx], bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (io->vel_out && !vel_copy)
+      cudaMemcpyAsync(io->vel_out, c->vel[nx], bytes, cudaMemcpyDeviceToHost, c->stream);
     cudaStreamWaitEvent(c->stream, c->io_ev[3], 0);  // join
   }
 }
@@ -819,7 +837,7 @@ bh_status bh_step_host(bh_ctx* c, const bh_params* prm, const float* pos_m4_in, 
   cudaSetDevice(c->device);
   if (st) std::memset(st, 0, sizeof(*st));
   if (c->n == 0) return BH_OK;
-  const HostIO io{pos_m4_in, vel4_in, pos_m4_out, vel4_out};
+  const HostIO io{pos_m4_in, vel4_in, pos_m4_out, vel4_out, mapped_float4(vel4_out)};
   if (!(pinned(pos_m4_in) && pinned(vel4_in) && pinned(pos_m4_out) && pinned(vel4_out))) {
     // pageable buffers cannot be captured: copy, step, copy in order on the context's stream
     const size_t bytes = sizeof(float4) * c->n;
@@ -993,10 +1011,12 @@ void enqueue_batch_step(bh_ctx* c, const bh_params& p, const HostIO* io, bool ma
   mark(6);
   bh::launch_upsweep(c, n, p.leaf_capacity, p.multipole, true);
   mark(7);
-  bh::launch_walk(c, n, (float)p.theta, (float)p.eps, p.multipole, c->acc, c->vel[nx], 0.5f * dt, true);
+  float4* vel_copy = io ? io->vel_out_dev : nullptr;
+  bh::launch_walk(c, n, (float)p.theta, (float)p.eps, p.multipole, c->acc, c->vel[nx], 0.5f * dt, true, vel_copy);
   mark(8);
   if (io) {
-    if (io->vel_out) cudaMemcpyAsync(io->vel_out, c->vel[nx], bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (io->vel_out && !vel_copy)
+      cudaMemcpyAsync(io->vel_out, c->vel[nx], bytes, cudaMemcpyDeviceToHost, c->stream);
     cudaStreamWaitEvent(c->stream, c->io_ev[3], 0);  // join
   }
 }
@@ -1208,7 +1228,7 @@ bh_status bh_batch_step_host(bh_ctx* c, const bh_params* prm, const float* pos_m
   cudaSetDevice(c->device);
   if (st) std::memset(st, 0, sizeof(*st));
   if (c->n == 0) return BH_OK;
-  const HostIO io{pos_m4_in, vel4_in, pos_m4_out, vel4_out};
+  const HostIO io{pos_m4_in, vel4_in, pos_m4_out, vel4_out, mapped_float4(vel4_out)};
   if (!(pinned(pos_m4_in) && pinned(vel4_in) && pinned(pos_m4_out) && pinned(vel4_out))) {
     const size_t bytes = sizeof(float4) * c->n;
     if (pos_m4_in) cudaMemcpyAsync(c->pos[c->cur], pos_m4_in, bytes, cudaMemcpyHostToDevice, c->stream);

@@ -272,8 +272,10 @@ void launch_sys_keys(bh_ctx* c, const uint32_t* vals, int n, uint64_t* k2);
 void launch_gather_tree_keys(bh_ctx* c, const uint32_t* tslot, int n, const float4* pos,
                              const uint64_t* key_by_slot, float4* tpos, uint64_t* tkey);
 void launch_hash(bh_ctx* c);
+// vel_copy (optional, with vel_kick): a second destination of the kicked velocities, such as a
+// caller's mapped pinned host buffer
 void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc_slot, float4* vel_kick,
-                 float half_dt, bool batch = false);
+                 float half_dt, bool batch = false, float4* vel_copy = nullptr);
 void launch_lookup(bh_ctx* c, uint64_t key, int* out_index);
 void launch_walk_record(bh_ctx* c, int n, float theta, float eps, float4* acc_slot, float4* vel_kick, float half_dt,
                         Chunk* tape, unsigned* tape_count, int tape_cap);

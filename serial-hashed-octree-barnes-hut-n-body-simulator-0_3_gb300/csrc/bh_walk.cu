@@ -240,6 +240,7 @@ __global__ __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) void k_walk(const W
                                                    const uint32_t* __restrict__ tslot, int n, float theta2,
                                                    float eps2, float4* __restrict__ acc_slot,
                                                    float4* __restrict__ vel_kick, float half_dt,
+                                                   float4* __restrict__ vel_copy,
                                                    const int4* __restrict__ groups, int ngroups_table, int gsize,
                                                    Counters* __restrict__ ctr, uint32_t* __restrict__ err,
                                                    Chunk* __restrict__ tape = nullptr,
@@ -524,6 +525,9 @@ __global__ __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) void k_walk(const W
         v.y += ay * half_dt;
         v.z += az * half_dt;
         vel_kick[slot] = v;
+        // a second copy of the kicked velocity (the caller's mapped pinned buffer of a host-IO
+        // step: the download then rides on the walk instead of following it)
+        if (vel_copy) vel_copy[slot] = v;
       }
     }
     tot_cell += (unsigned long long)cnt_cell;
@@ -570,11 +574,11 @@ int walk_grid() {
 
 template <bool kQuad, bool kSelf, class Cfg = CfgDefault>
 void launch_walk_t(bh_ctx* c, int n, float theta2, float eps2, float4* acc_slot, float4* vel_kick, float half_dt,
-                   bool batch, int gsize = 32) {
+                   float4* vel_copy, bool batch, int gsize = 32) {
   const int ngroups = batch ? c->ngroups : (n + gsize - 1) / gsize;
   const int grid = min(walk_grid<kQuad, kSelf, false, Cfg>(), ngroups / Cfg::kWarps + 1);
   k_walk<kQuad, kSelf, false, Cfg><<<grid, Cfg::kThreads, 0, c->stream>>>(
-      c->wnode, c->tpos, c->tslot, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch ? c->groups : nullptr,
+      c->wnode, c->tpos, c->tslot, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch ? c->groups : nullptr,
       c->ngroups, gsize, c->counters, c->err);
 }
 
@@ -603,20 +607,30 @@ WalkVariant variant_info(int group = 32) {
 }
 
 void launch_quad_variant(bh_ctx* c, int v, int n, float theta2, float eps2, float4* acc_slot, float4* vel_kick,
-                         float half_dt, bool batch) {
+                         float half_dt, float4* vel_copy, bool batch) {
   switch (v) {
-    case 1: launch_walk_t<true, false, Cfg1>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
-    case 2: launch_walk_t<true, false, Cfg2>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
-    case 3: launch_walk_t<true, false, Cfg3>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
-    case 4: launch_walk_t<true, false, Cfg4>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
-    case 5: launch_walk_t<true, false, Cfg5>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
-    case 6: launch_walk_t<true, false, Cfg6>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
-    case 7: launch_walk_t<true, false, Cfg7>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
-    case 8: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, 16); break;
-    case 9: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, 8); break;
-    case 10: launch_walk_t<true, false, Cfg2>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, 16); break;
-    case 11: launch_walk_t<true, false, Cfg2>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, 8); break;
-    default: launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch); break;
+    case 1: launch_walk_t<true, false, Cfg1>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch); break;
+    case 2: launch_walk_t<true, false, Cfg2>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch); break;
+    case 3: launch_walk_t<true, false, Cfg3>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch); break;
+    case 4: launch_walk_t<true, false, Cfg4>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch); break;
+    case 5: launch_walk_t<true, false, Cfg5>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch); break;
+    case 6: launch_walk_t<true, false, Cfg6>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch); break;
+    case 7: launch_walk_t<true, false, Cfg7>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch); break;
+    case 8:
+      launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch, 16);
+      break;
+    case 9:
+      launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch, 8);
+      break;
+    case 10:
+      launch_walk_t<true, false, Cfg2>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch, 16);
+      break;
+    case 11:
+      launch_walk_t<true, false, Cfg2>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch, 8);
+      break;
+    default:
+      launch_walk_t<true, false, CfgDefault>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch);
+      break;
   }
 }
 
@@ -646,7 +660,7 @@ void launch_walk_variant(bh_ctx* c, int v, int n, float theta, float eps, float4
   if (n <= 0) return;
   cudaMemsetAsync(&c->counters->group_next, 0, sizeof(unsigned), c->stream);
   c->launches += 1;
-  launch_quad_variant(c, v, n, theta * theta, eps * eps, acc_out, nullptr, 0.f, batch);
+  launch_quad_variant(c, v, n, theta * theta, eps * eps, acc_out, nullptr, 0.f, nullptr, batch);
 }
 
 // Occupancy queries done once per process, before any stream capture.
@@ -673,7 +687,7 @@ void walk_init() {
 constexpr int kLiteralMinGroup = BH_LITERAL_MIN_GROUP;
 
 void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc_slot, float4* vel_kick,
-                 float half_dt, bool batch) {
+                 float half_dt, bool batch, float4* vel_copy) {
   if (n <= 0) return;
   cudaMemsetAsync(&c->counters->group_next, 0, sizeof(unsigned), c->stream);
   c->launches += 1;
@@ -682,9 +696,9 @@ void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc
   const bool self = !(eps2 > 0.f);
   if (quad) {
     if (self)
-      launch_walk_t<true, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
+      launch_walk_t<true, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch);
     else
-      launch_quad_variant(c, c->walk_variant, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch);
+      launch_quad_variant(c, c->walk_variant, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch);
   } else {
     // the literal walk has no tuned variants: its group size follows N, the largest of 32, 16,
     // 8 and 4 bodies that still gives at least 1024 groups (about seven warps per SM; the tuned
@@ -692,9 +706,9 @@ void launch_walk(bh_ctx* c, int n, float theta, float eps, int mode, float4* acc
     int gsize = 32;
     while (gsize > kLiteralMinGroup && (n + gsize - 1) / gsize < 1024) gsize /= 2;
     if (self)
-      launch_walk_t<false, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, gsize);
+      launch_walk_t<false, true>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch, gsize);
     else
-      launch_walk_t<false, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, batch, gsize);
+      launch_walk_t<false, false>(c, n, theta2, eps2, acc_slot, vel_kick, half_dt, vel_copy, batch, gsize);
   }
 }
 
@@ -712,8 +726,9 @@ void launch_walk_record(bh_ctx* c, int n, float theta, float eps, float4* acc_sl
   c->launches += 1;
   const int grid = min(walk_grid<true, false, true, CfgDefault>(), ((n + 31) / 32) / kWarps + 1);
   k_walk<true, false, true><<<grid, kThreads, 0, c->stream>>>(c->wnode, c->tpos, c->tslot, n, theta * theta,
-                                                              eps * eps, acc_slot, vel_kick, half_dt, nullptr, 0,
-                                                              32, c->counters, c->err, tape, tape_count, tape_cap);
+                                                              eps * eps, acc_slot, vel_kick, half_dt, nullptr,
+                                                              nullptr, 0, 32, c->counters, c->err, tape, tape_count,
+                                                              tape_cap);
 }
 
 }  // namespace bh

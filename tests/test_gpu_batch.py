@@ -74,8 +74,10 @@ def test_batch_set_rejects_bad_offsets(bh):
 
 def test_batch_step_host_matches_batch_step(bh):
     """bh_batch_step_host (host copies beside the batched step) follows bh_batch_step's
-    trajectory bit for bit, with page-locked and with pageable buffers, also after a plain step
-    on the same context (its step graphs must not be reused for the ensemble)."""
+    trajectory bit for bit, with page-locked buffers (velocities stored by the walk's kick into
+    the mapped output), with a velocity output off a 16-byte boundary (downloaded after the
+    walk), with pageable buffers, and after a plain step on the same context (its step graphs
+    must not be reused for the ensemble)."""
     pm, vel, off = ensemble(bh, 23, 3, 50, 2000)
     n = len(pm)
     prm = bh.default_params(theta=0.6, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1, edge_factor=2.0)
@@ -88,8 +90,10 @@ def test_batch_step_host_matches_batch_step(bh):
             p, v, _ = a.get_bodies()
             ref.append((p.copy(), v.copy()))
     bufs = [bh.PinnedArray((n, 4)) for _ in range(4)]
+    spare = bh.PinnedArray((n + 1, 4))
+    unaligned_vo = spare.array.reshape(-1)[1:1 + 4 * n].reshape(n, 4)
     try:
-        for mode in ("pinned", "pageable", "after_plain"):
+        for mode in ("pinned", "unaligned", "pageable", "after_plain"):
             with bh.Simulation(n) as b:
                 if mode == "after_plain":
                     b.set_bodies(pm, vel)
@@ -103,6 +107,8 @@ def test_batch_step_host_matches_batch_step(bh):
                         p, v = po, vo
                     else:
                         pi, vi, po, vo = (x.array for x in bufs)
+                        if mode == "unaligned":
+                            vo = unaligned_vo
                         pi[:] = p
                         vi[:] = v
                         b.batch_step_host(prm, pi, vi, po, vo)
@@ -111,6 +117,8 @@ def test_batch_step_host_matches_batch_step(bh):
     finally:
         for x in bufs:
             x.free()
+        unaligned_vo = None
+        spare.free()
 
 
 def test_batch_at_the_system_limit(bh):

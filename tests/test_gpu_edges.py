@@ -136,13 +136,16 @@ def test_reset_same_count_replays_identically(bh):
             assert np.array_equal(g, r)
 
 
-@pytest.mark.parametrize("n", [5000, 70000])
-def test_step_host_matches_step(bh, n):
+@pytest.mark.parametrize("n,multipole,eps", [(5000, 1, 0.01), (70000, 1, 0.01), (4444, 0, 0.0)])
+def test_step_host_matches_step(bh, n, multipole, eps):
     """bh_step_host (upload, step, download; copies overlapped with page-locked buffers) follows
-    the same trajectory as bh_step, bit for bit: with page-locked buffers, with buffers that
-    change between calls (re-capture), with pageable numpy arrays, and with no copies at all."""
+    the same trajectory as bh_step, bit for bit: with page-locked buffers (the walk's kick
+    writes the velocities into the mapped output buffer), with buffers that change between calls
+    (re-capture), with a velocity output 4 bytes off a 16-byte boundary (no direct stores: the
+    download follows the walk), with pageable numpy arrays, and with no copies at all; for the
+    quadrupole walk and for the literal walk without softening."""
     pm, vel = bh.plummer(8, n)
-    prm = bh.default_params(theta=0.5, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1, edge_factor=2.0)
+    prm = bh.default_params(theta=0.5, eps=eps, dt=1e-3, leaf_capacity=8, multipole=multipole, edge_factor=2.0)
     steps = 6
     ref = []
     with bh.Simulation(n) as a:
@@ -152,8 +155,10 @@ def test_step_host_matches_step(bh, n):
             p, v, _ = a.get_bodies()
             ref.append((p.copy(), v.copy()))
     bufs = [[bh.PinnedArray((n, 4)) for _ in range(4)] for _ in range(2)]
+    spare = bh.PinnedArray((n + 1, 4))
+    unaligned_vo = spare.array.reshape(-1)[1:1 + 4 * n].reshape(n, 4)
     try:
-        for mode in ("pinned", "alternating", "pageable", "none"):
+        for mode in ("pinned", "alternating", "unaligned", "pageable", "none"):
             with bh.Simulation(n) as b:
                 b.set_bodies(pm, vel)
                 p, v = pm.copy(), vel.copy()
@@ -167,6 +172,8 @@ def test_step_host_matches_step(bh, n):
                         p, v = po, vo
                     else:
                         pi, vi, po, vo = (x.array for x in bufs[k % 2 if mode == "alternating" else 0])
+                        if mode == "unaligned":
+                            vo = unaligned_vo
                         pi[:] = p
                         vi[:] = v
                         b.step_host(prm, pi, vi, po, vo)
@@ -176,6 +183,8 @@ def test_step_host_matches_step(bh, n):
         for s in bufs:
             for x in s:
                 x.free()
+        unaligned_vo = None
+        spare.free()
 
 
 def test_caller_stream(bh):
