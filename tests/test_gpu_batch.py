@@ -75,9 +75,9 @@ def test_batch_set_rejects_bad_offsets(bh):
 def test_batch_step_host_matches_batch_step(bh):
     """bh_batch_step_host (host copies beside the batched step) follows bh_batch_step's
     trajectory bit for bit, with page-locked buffers (velocities stored by the walk's kick into
-    the mapped output), with a velocity output off a 16-byte boundary (downloaded after the
-    walk), with pageable buffers, and after a plain step on the same context (its step graphs
-    must not be reused for the ensemble)."""
+    the mapped output), with the same arrays as input and output, with a velocity output off a
+    16-byte boundary (downloaded after the walk), with pageable buffers, and after a plain step
+    on the same context (its step graphs must not be reused for the ensemble)."""
     pm, vel, off = ensemble(bh, 23, 3, 50, 2000)
     n = len(pm)
     prm = bh.default_params(theta=0.6, eps=0.01, dt=1e-3, leaf_capacity=8, multipole=1, edge_factor=2.0)
@@ -93,7 +93,7 @@ def test_batch_step_host_matches_batch_step(bh):
     spare = bh.PinnedArray((n + 1, 4))
     unaligned_vo = spare.array.reshape(-1)[1:1 + 4 * n].reshape(n, 4)
     try:
-        for mode in ("pinned", "unaligned", "pageable", "after_plain"):
+        for mode in ("pinned", "inplace", "unaligned", "pageable", "after_plain"):
             with bh.Simulation(n) as b:
                 if mode == "after_plain":
                     b.set_bodies(pm, vel)
@@ -109,6 +109,8 @@ def test_batch_step_host_matches_batch_step(bh):
                         pi, vi, po, vo = (x.array for x in bufs)
                         if mode == "unaligned":
                             vo = unaligned_vo
+                        if mode == "inplace":
+                            po, vo = pi, vi
                         pi[:] = p
                         vi[:] = v
                         b.batch_step_host(prm, pi, vi, po, vo)

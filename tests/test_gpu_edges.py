@@ -140,7 +140,8 @@ def test_reset_same_count_replays_identically(bh):
 def test_step_host_matches_step(bh, n, multipole, eps):
     """bh_step_host (upload, step, download; copies overlapped with page-locked buffers) follows
     the same trajectory as bh_step, bit for bit: with page-locked buffers (the walk's kick
-    writes the velocities into the mapped output buffer), with buffers that change between calls
+    writes the velocities into the mapped output buffer), with the same page-locked arrays as
+    input and output (the per-frame pattern), with buffers that change between calls
     (re-capture), with a velocity output 4 bytes off a 16-byte boundary (no direct stores: the
     download follows the walk), with pageable numpy arrays, and with no copies at all; for the
     quadrupole walk and for the literal walk without softening."""
@@ -158,7 +159,7 @@ def test_step_host_matches_step(bh, n, multipole, eps):
     spare = bh.PinnedArray((n + 1, 4))
     unaligned_vo = spare.array.reshape(-1)[1:1 + 4 * n].reshape(n, 4)
     try:
-        for mode in ("pinned", "alternating", "unaligned", "pageable", "none"):
+        for mode in ("pinned", "inplace", "alternating", "unaligned", "pageable", "none"):
             with bh.Simulation(n) as b:
                 b.set_bodies(pm, vel)
                 p, v = pm.copy(), vel.copy()
@@ -174,6 +175,8 @@ def test_step_host_matches_step(bh, n, multipole, eps):
                         pi, vi, po, vo = (x.array for x in bufs[k % 2 if mode == "alternating" else 0])
                         if mode == "unaligned":
                             vo = unaligned_vo
+                        if mode == "inplace":
+                            po, vo = pi, vi
                         pi[:] = p
                         vi[:] = v
                         b.step_host(prm, pi, vi, po, vo)
