@@ -172,30 +172,20 @@ __device__ __forceinline__ uint64_t tree_key(float4 p, const Geom& g) {
   return (1ull << 63) | (spread_bits(kx) << 2) | (spread_bits(ky) << 1) | spread_bits(kz);
 }
 
-// Tree geometry from the root cube and its two quotients tscale = 2^21 / tedge and
-// cm_edge = max_a |tc_a| / tedge (both correctly rounded).
-__device__ __forceinline__ void fill_tree_geom_q(Geom& g, const double tc[3], double tedge, double tscale,
-                                                 double cm_edge) {
+__device__ __forceinline__ void fill_tree_geom(Geom& g, const double tc[3], double tedge) {
   g.tc[0] = tc[0];
   g.tc[1] = tc[1];
   g.tc[2] = tc[2];
   g.tedge = tedge;
-  g.tscale = tscale;
-  g.tmargin = 0x1p-20 * (1.0 + cm_edge);
+  g.tscale = __ddiv_rn(2097152.0, tedge);
+  double cm = fmax(fabs(tc[0]), fmax(fabs(tc[1]), fabs(tc[2])));
+  g.tmargin = 0x1p-20 * (1.0 + cm / tedge);
   // float-float copies for the key fast paths (size and frac are set by every caller first)
   ff_split(g.size, g.size_hi, g.size_lo);
   ff_split(g.frac, g.frac_hi, g.frac_lo);
   for (int a = 0; a < 3; ++a) ff_split(tc[a], g.tc_hi[a], g.tc_lo[a]);
   ff_split(g.tscale, g.tscale_hi, g.tscale_lo);
   g.tmargin_f = __double2float_rn(g.tmargin);
-}
-
-__device__ __forceinline__ double max_abs3(const double v[3]) {
-  return fmax(fabs(v[0]), fmax(fabs(v[1]), fabs(v[2])));
-}
-
-__device__ __forceinline__ void fill_tree_geom(Geom& g, const double tc[3], double tedge) {
-  fill_tree_geom_q(g, tc, tedge, __ddiv_rn(2097152.0, tedge), __ddiv_rn(max_abs3(tc), tedge));
 }
 
 // ---------------------------------------------------------------------------------------
@@ -249,10 +239,8 @@ __global__ __launch_bounds__(kThreads) void k_bounds_partial(const float4* __res
 // shuffle tree; deterministic, and only ~15 dependent FP64 additions deep): centre = sum *
 // (1 / N) (Vec3D::operator/=, src/MathUtils.cpp:81-90), size = max(0, max_a (max_i |p_ia| -
 // c_a)). fl(|p| - c) is monotone in |p|, so the maximum over bodies of the rounded differences
-// equals the rounded difference of the maximum. inv_n = 1 / N is correctly rounded by the host
-// (the same value as a device division), and the three quotients of the geometry are taken at
-// once on three lanes: the FP64 divisions are the slow part of this one-warp kernel.
-__global__ void k_bounds_final(const double* __restrict__ partial, int blocks, double inv_n, double edge_factor,
+// equals the rounded difference of the maximum.
+__global__ void k_bounds_final(const double* __restrict__ partial, int blocks, int n, double edge_factor,
                                Geom* __restrict__ g) {
   const int lane = threadIdx.x;
   double s[3] = {0, 0, 0}, m[3] = {0, 0, 0};
@@ -267,32 +255,22 @@ __global__ void k_bounds_final(const double* __restrict__ partial, int blocks, d
       s[a] = __dadd_rn(s[a], __shfl_down_sync(0xffffffffu, s[a], o));
       m[a] = fmax(m[a], __shfl_down_sync(0xffffffffu, m[a], o));
     }
-  // lane 0's totals on every lane
-  double c[3];
-  for (int a = 0; a < 3; ++a) {
-    c[a] = __shfl_sync(0xffffffffu, s[a], 0);
-    m[a] = __shfl_sync(0xffffffffu, m[a], 0);
+  if (lane != 0) return;
+  double c[3] = {s[0], s[1], s[2]};
+  double nn = (double)n;
+  if (nn != 0) {
+    double inv = __ddiv_rn(1.0, nn);
+    for (int a = 0; a < 3; ++a) c[a] = __dmul_rn(c[a], inv);
   }
-  if (inv_n != 0)
-    for (int a = 0; a < 3; ++a) c[a] = __dmul_rn(c[a], inv_n);
   double S = 0;
   for (int a = 0; a < 3; ++a) {
-    const double v = __dsub_rn(m[a], c[a]);
+    double v = __dsub_rn(m[a], c[a]);
     if (v > S) S = v;
   }
-  const double tedge = __dmul_rn(S, edge_factor);
-  // lane 0: 2^21 / (2 S); lane 1: 2^21 / tedge; lane 2: max_a |c_a| / tedge
-  const double num = lane == 2 ? max_abs3(c) : 2097152.0;
-  const double den = lane == 0 ? __dmul_rn(2.0, S) : tedge;
-  const double q = __ddiv_rn(num, den);
-  const double frac = q;
-  const double tscale = __shfl_sync(0xffffffffu, q, 1);
-  const double cm_edge = __shfl_sync(0xffffffffu, q, 2);
-  if (lane != 0) return;
   for (int a = 0; a < 3; ++a) g->center[a] = c[a];
   g->size = S;
-  g->frac = frac;
-  fill_tree_geom_q(*g, c, tedge, tscale, cm_edge);
+  g->frac = __ddiv_rn(2097152.0, __dmul_rn(2.0, S));
+  fill_tree_geom(*g, c, __dmul_rn(S, edge_factor));
 }
 
 __global__ void k_set_geom(Geom* __restrict__ g, double c0, double c1, double c2, double S, double t0, double t1,
@@ -1420,8 +1398,7 @@ inline int grid_for(long long n) { return (int)((n + kThreads - 1) / kThreads); 
 void launch_bounds(bh_ctx* c, const float4* pos, int n, double edge_factor) {
   c->launches += 2;
   k_bounds_partial<<<c->bounds_blocks, kThreads, 0, c->stream>>>(pos, n, c->bounds_partial);
-  const double inv_n = n > 0 ? 1.0 / (double)n : 0.0;  // IEEE division: correctly rounded
-  k_bounds_final<<<1, 32, 0, c->stream>>>(c->bounds_partial, c->bounds_blocks, inv_n, edge_factor, c->geom);
+  k_bounds_final<<<1, 32, 0, c->stream>>>(c->bounds_partial, c->bounds_blocks, n, edge_factor, c->geom);
 }
 
 void launch_set_geom(bh_ctx* c, const double center[3], double size, const double tcenter[3], double tedge) {
