@@ -903,17 +903,22 @@ __global__ __launch_bounds__(kPBThreads) void k_nodes_write(const uint64_t* __re
 // their cells adjacent, so a node's cell ends where its next sibling's starts, and a last
 // child's where its parent's ends (the climb passes only through last children: about 1.3
 // nodes on average). The last child of each parent (the next node has another parent) also
-// counts its siblings from the parent's first child and ORs their digits.
+// counts its siblings from the parent's first child and ORs their digits. The upsweep's arrival
+// counters are zeroed here as well (the parent links it needs are k_nodes_write's), so the
+// all-depths build needs no separate k_upsweep_links.
 __global__ __launch_bounds__(kThreads) void k_nodes_link(const int* __restrict__ level_bounds,
                                                          const uint64_t* __restrict__ nkey,
                                                          const int* __restrict__ nparent, int2* __restrict__ nrange,
                                                          WalkNode* __restrict__ wn, uint8_t* __restrict__ childbyte,
+                                                         uint32_t* __restrict__ arrived,
                                                          const uint32_t* __restrict__ err) {
   if (*err & kErrNodes) return;
   const int m = level_bounds[kLevels];
   const int n = nrange[0].y;
+  if (blockIdx.x == 0 && threadIdx.x == 0) arrived[0] = 0u;
   auto last_child = [&](int j) { return j + 1 >= m || nparent[j + 1] != nparent[j]; };
   for (int j = 1 + blockIdx.x * kThreads + threadIdx.x; j < m; j += gridDim.x * kThreads) {
+    arrived[j] = 0u;
     const bool last = last_child(j);
     int a = j;
     bool up = last;
@@ -1454,8 +1459,12 @@ void launch_gather_tree(bh_ctx* c, const uint32_t* tslot, int n, const float4* p
 // Function attributes set once per process, before any stream capture (none at present).
 void tree_init() {}
 
+// Single trees with leaves of at most kPBMaxLeaf bodies: every depth at once (k_nodes_*), parent
+// links and the upsweep's counters included; otherwise the level build.
+bool builds_all_depths(int n, int leaf_cap, bool batch) { return !batch && n >= 1 && leaf_cap <= kPBMaxLeaf; }
+
 void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
-  if (!batch && n >= 1 && leaf_cap <= kPBMaxLeaf) {
+  if (builds_all_depths(n, leaf_cap, batch)) {
     // every depth at once: counts per tile and depth (in lb_level), their scans (totals in
     // level_tile_ctr), the node records (start depths of each body in vals[1], free after the
     // sorts), then child counts and bytes
@@ -1471,7 +1480,7 @@ void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
                                                         c->level_bounds, (long long)c->node_cap, c->err);
     const int lgrid = (int)std::min<size_t>((size_t)c->sms * 8, (c->node_cap + kThreads - 1) / kThreads);
     k_nodes_link<<<lgrid, kThreads, 0, c->stream>>>(c->level_bounds, c->nkey, c->nparent, c->nrange, c->wnode,
-                                                    c->nchildbyte, c->err);
+                                                    c->nchildbyte, c->narrived, c->err);
     return;
   }
   c->launches += 1 + kLevels;
@@ -1496,15 +1505,19 @@ void launch_build(bh_ctx* c, int n, int leaf_cap, bool batch) {
 constexpr int kUpsweepPrefetchMaxBodies = BH_UPSWEEP_PREFETCH_MAX;
 
 void launch_upsweep(bh_ctx* c, int n, int leaf_cap, int mode, bool batch) {
-  (void)leaf_cap;
   if (n <= 0) return;
   // a thread for every two bodies, about one per node or more at leaf capacity >= 2 (the climbs
   // want a thread per leaf: at N = 2^22 a fixed 8 blocks per SM took 0.39 ms, this 0.27 ms, the
   // level-by-level pass it replaces 0.29 ms; at N = 2^25 a fixed 32 blocks per SM took 2.65 ms,
   // this 1.54 ms)
   const int grid = std::max(c->sms * 8, (n / 2 + kThreads - 1) / kThreads);
-  c->launches += 2;
-  k_upsweep_links<<<grid, kThreads, 0, c->stream>>>(c->level_bounds, c->wnode, c->nparent, c->narrived, c->err);
+  // parent links and zeroed arrival counters: written by the all-depths build itself, or here
+  // after the level build
+  if (!builds_all_depths(n, leaf_cap, batch)) {
+    c->launches += 1;
+    k_upsweep_links<<<grid, kThreads, 0, c->stream>>>(c->level_bounds, c->wnode, c->nparent, c->narrived, c->err);
+  }
+  c->launches += 1;
   // the prefetching climb holds eight children's records in registers (one block per SM): two
   // threads per body there (about one per node at leaf capacity 1), at least a block per SM
   const bool prefetch = n <= kUpsweepPrefetchMaxBodies;
