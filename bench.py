@@ -516,7 +516,7 @@ def run_ours(args, w, dist):
     line = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (keys, bounds, tree geometry and upsweep in f64)",
+        "vs_baseline": None, "dtype": "f32 (keys, bounds and tree geometry in f64; node masses and centres in float-float)",
         "data": "synthetic", "impl": "ours",
         "config": workload_config(args, w),
         "timing": "per-step CUDA events on the library stream around each bh_step call (graph launch "
